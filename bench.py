@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark of the staggered-grid elastic FDTD time loop (one JSON line on stdout).
+
+Workload (default): the orthorhombic layered model, 320 x 320 x 256 cells, FP32, 4000 time steps,
+64 surface receivers x 3 components (seeded synthetic inputs, see elanfmt_gb300/inputs.py).
+One bench "step" is one full run of the workload through libewfd.so with the inputs resident in
+HBM; `value` = cell-updates per second over the K timed runs (CUDA events on the solver's stream,
+max over ranks).  The working set (~2.6 GB) is far larger than L2, so no flush is needed.
+
+Also reported: `e2e` (the same runs through the C ABI from pinned host buffers, H2D of every
+input and D2H of the seismograms inside the timed region), `roofline` (algorithmic bytes of the
+dominant kernel / its CUDA-event duration, against MEASURED_PEAKS.json), `cpu_baseline` (the
+FP64 C loop of the reference scheme, i.e. the CPU oracle, on the host cores, bounded sample),
+`reference_gpu` (the reference's own kernels, compiled from its sources, on the same GPU and
+workload), `clocks` (nvidia-smi sampled during the timed region) and `gpu_launches`.
+
+--impl reference times the reference's CPU implementation of the path (the oracle port, FP64,
+all host threads) on the same workload and metric, each step a bounded sample of time steps.
+Multi-GPU: replicas only (independent runs, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s & % HBM roofline; Green's-fn sets/s surrogate vs FDTD @<=1e-3 L2"
+UNIT = "Gcell-updates/s"
+
+# compulsory DRAM bytes per cell-update, FP32 (each state field read+written once, each material
+# field read once, separable damping ~0): whole step, and per kernel of the two-kernel step
+STEP_BYTES = {"ortho": 120, "iso": 80}
+KERNEL_BYTES = {
+    "ortho": {"stress": 4 * (3 + 6 + 9 + 6), "velocity": 4 * (6 + 3 + 3 + 3)},
+    "iso": {"stress": 4 * (3 + 6 + 2 + 6), "velocity": 4 * (6 + 3 + 3)},
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ortho", choices=["ortho", "iso"])
+    ap.add_argument("--nt", type=int, default=0, help="time steps per run (default: the workload's)")
+    ap.add_argument("--size", type=str, default="", help="override grid, e.g. 128x128x96 (profiling runs)")
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e, cpu baseline, reference_gpu, kernel timing")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def workload(name: str, nt: int, size: str):
+    from elanfmt_gb300 import inputs as I
+
+    if name == "ortho":
+        nx, ny, nz = (int(v) for v in size.split("x")) if size else (320, 320, 256)
+        m = I.ortho_layered(nx=nx, ny=ny, nz=nz, nt=nt or 4000, src=(nx // 2, ny // 2, nz // 2),
+                            rec_coords=None if (nx, ny) == (320, 320) else
+                            [int(round(v)) for v in (nx * (0.125 + 0.75 * q / 7) for q in range(8))])
+        desc = f"orthorhombic layered {nx}x{ny}x{nz}, {m.nt} steps, 12 layers, 15-cell PML, lune MT, Ricker 1.5 Hz"
+    else:
+        n = int(size.split("x")[0]) if size else 128
+        m = I.iso_homogeneous(n=n, nt=nt or 1000)
+        desc = f"isotropic homogeneous {n}^3, {m.nt} steps, 10-cell PML, DC MT, Ricker 2 Hz"
+    return m, desc
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p))["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, workload_name: str):
+    """DRAM bytes per cell of a kernel from the committed ncu summary (None if absent)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        kv = dict(t.split("=", 1) for t in line.split() if "=" in t)
+        if kv.get("kernel") == kernel and kv.get("workload") == workload_name:
+            return float(kv["dram_bytes_per_cell"])
+    return None
+
+
+def cpu_baseline(m, seconds: float) -> dict:
+    """FP64 C loop of the reference scheme (the CPU oracle) on this host's cores, bounded sample."""
+    from elanfmt_gb300 import fields as F
+    from oracle import oracle as O
+
+    r = O.Runner(m, F.PREC_F64)
+    t = time.perf_counter()
+    r.step(1)
+    one = time.perf_counter() - t
+    n = max(1, min(m.nt - 1, int(seconds / max(one, 1e-6))))
+    t = time.perf_counter()
+    r.step(n)
+    dt = time.perf_counter() - t
+    return {"value": m.cells * n / dt / 1e9, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+            "sample": f"{n} time steps of the full {m.nx}x{m.ny}x{m.nz} grid after 1 warm-up step, FP64, "
+                      f"{dt:.1f} s"}
+
+
+def reference_gpu(m, nsteps: int) -> dict | None:
+    """The reference's own kernels (stock build) on the same workload, timed with its own per-
+    launch synchronisation (OK4:487-498 / ANISO:521-550)."""
+    import copy
+
+    import numpy as np
+    import torch
+
+    from elanfmt_gb300 import fields as F
+    from elanfmt_gb300.inputs import separable_weights
+    from oracle import refrun as R
+
+    if not R.available(m.model, "stock"):
+        return None
+    mm = copy.copy(m)
+    mm.receivers = None
+    if m.model == F.MODEL_ORTHO:
+        d = m.damping_arrays
+        if F.D_W3D not in d:
+            mm.damping_arrays = {F.D_W3D: separable_weights(d[F.D_WX], d[F.D_WY], d[F.D_WZ])}
+        xs, ys, zs = (int(v) - 1 for v in m.sources[0, 1:4])
+        mm.set_moment_tensor(np.array(F.ANISO_LEGACY_MT), xs, ys, zs, 1)
+    r = R.RefRunner(mm, "stock")
+    try:
+        r.run(5)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r.run(nsteps)
+        dt = time.perf_counter() - t
+    finally:
+        r.close()
+    return {"value": m.cells * nsteps / dt / 1e9, "unit": UNIT, "steps": nsteps,
+            "what": "reference kernels compiled from the reference sources (-O3, sm_103a), launch + sync per kernel"}
+
+
+def main():
+    args = parse()
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        return main_reference(args)
+
+    from elanfmt_gb300 import fields as F
+    from elanfmt_gb300.solver import Solver
+
+    torch.cuda.set_device(local)
+    m, desc = workload(args.workload, args.nt, args.size)
+    nt = m.nt
+    s = Solver.from_model(m)
+
+    for _ in range(args.warmup):
+        s.reset()
+        s.run(nt)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = Clocks(local)
+    clk.start()
+    ms = []
+    for _ in range(args.steps):
+        s.reset()
+        ms.append(s.run(nt))
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_ms = sum(ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    units = m.cells * nt * args.steps * world
+    value = units / (total_ms * 1e-3) / 1e9
+    launches = s.launches_per_step() * nt * args.steps
+
+    peak, peak_kind = peaks()
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": nt, "receivers": len(m.receivers),
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (working set ~%.1f GB)" % (m.cells * 4 * 21 / 1e9)},
+        "gpu_launches": launches,
+    }
+    step_frac = value * STEP_BYTES[args.workload] / peak
+    out["step_roofline"] = {"bytes_per_cell": STEP_BYTES[args.workload], "achieved": round(value * STEP_BYTES[args.workload], 1),
+                            "peak": peak, "unit": "GB/s", "frac": round(step_frac, 4), "peak_kind": peak_kind}
+    if clocks:
+        out["clocks"] = clocks
+
+    if not args.no_extras and rank == 0:
+        # per-kernel CUDA-event timing on the solver's stream
+        s.reset()
+        kt = s.time_kernels(min(200, nt))
+        kb = KERNEL_BYTES[args.workload]
+        kernels = {}
+        for k in ("stress", "velocity"):
+            achieved = kb[k] * m.cells / (kt[k] * 1e-3) / 1e9
+            kernels[k] = {"ms": round(kt[k], 4), "bytes_per_cell": kb[k], "achieved_gbs": round(achieved, 1),
+                          "frac": round(achieved / peak, 4)}
+        dom = max(("stress", "velocity"), key=lambda k: kt[k])
+        tr = ncu_traffic(f"k_{dom}", args.workload)
+        out["roofline"] = {"kernel": f"k_{dom}", "bound": "hbm", "achieved": kernels[dom]["achieved_gbs"],
+                           "peak": peak, "unit": "GB/s", "frac": kernels[dom]["frac"],
+                           "traffic": None if tr is None else round(tr * m.cells),
+                           "algorithmic_bytes": kb[dom] * m.cells, "peak_kind": peak_kind}
+        out["kernels"] = kernels | {"inject_ms": round(kt["inject"], 4), "record_ms": round(kt["record"], 4)}
+        out["e2e"] = e2e(s, m, args.steps)
+        out["reference_gpu"] = reference_gpu(m, 200 if m.cells > 10_000_000 else 500)
+        out["cpu_baseline"] = cpu_baseline(m, args.cpu_seconds)
+    s.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def e2e(s, m, steps: int) -> dict:
+    """Through the C ABI with host buffers: every input H2D from pinned memory, the full run, the
+    seismograms D2H -- all inside the timed region."""
+    import numpy as np
+    import torch
+
+    pinned = []
+    for fid, arr in list(m.materials.items()) + list(m.damping_arrays.items()):
+        t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+        pinned.append((fid, t))
+    stf = torch.from_numpy(np.ascontiguousarray(m.stf, np.float64)).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for _, t in pinned) + stf.numel() * 8 + m.sources.size * 4 + \
+        m.source_coef.size * 8 + m.receivers.size * 4
+    trace = torch.empty((len(m.receivers), m.nt), dtype=torch.float64).pin_memory()
+    d2h = trace.numel() * 8
+    n = max(1, min(steps, 2))
+    times = []
+    for _ in range(n):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for fid, t in pinned:
+            s.set_field_ptr(fid, t.data_ptr(), t.numel(), t.element_size())
+        s._lib.ewf_set_stf(s._h, stf.data_ptr(), stf.numel())
+        s.set_sources(m.sources, m.source_coef)
+        s.set_receivers(m.receivers)
+        s.reset()
+        s.run(m.nt)
+        s._lib.ewf_get_seismograms(s._h, trace.data_ptr(), trace.numel())
+        t1 = time.perf_counter()
+        times.append(t1 - t0)
+    best = statistics.median(times)
+    return {"value": round(m.cells * m.nt / best / 1e9, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "runs": n, "seconds_per_step": round(best, 4)}
+
+
+def main_reference(args):
+    """The reference's CPU implementation of the path: the FP64 C loop of the reference scheme
+    (oracle port) on all host threads; each bench step is a bounded sample of time steps."""
+    from oracle import oracle as O
+
+    from elanfmt_gb300 import fields as F
+
+    m, desc = workload(args.workload, args.nt, args.size)
+    r = O.Runner(m, F.PREC_F64)
+    t = time.perf_counter()
+    r.step(1)
+    one = time.perf_counter() - t
+    per = max(1, min(20, int(6.0 / max(one, 1e-6))))
+    for _ in range(args.warmup):
+        r.step(per) if r.state.it + per < m.nt else None
+    times = []
+    for _ in range(args.steps):
+        if r.state.it + per >= m.nt:
+            r = O.Runner(m, F.PREC_F64)
+        t = time.perf_counter()
+        r.step(per)
+        times.append(time.perf_counter() - t)
+    total = sum(times)
+    value = m.cells * per * args.steps / total / 1e9
+    sample = f"{per} time steps of the full {m.nx}x{m.ny}x{m.nz} grid per bench step, FP64"
+    out = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": 0,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded)", "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": m.nt},
+           "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "gpu_launches": 0}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

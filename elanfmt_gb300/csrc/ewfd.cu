@@ -1,0 +1,874 @@
+// ewfd.cu -- host side of libewfd.so: handle, device memory, the time loop under CUDA graphs.
+//
+// Replaces the reference executable's main() (OK4:390-559, ANISO:391-608): instead of
+// compile-time grids, fixed file names and a launch + cudaDeviceSynchronize per kernel
+// (OK4:487-498), a handle owns the fields in the padded box layout, a stream, and a CUDA graph
+// that replays `graph_steps` time steps per launch; the step index lives on the device so the
+// same graph serves every chunk.
+#include "ewfd.h"
+#include "ewfd_internal.h"
+#include "ewfd_kernels.cuh"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace ewf;
+
+// ------------------------------------------------------------------------------------------
+// errors
+// ------------------------------------------------------------------------------------------
+static thread_local char g_err[512];
+
+int ewf_fail(int status, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return ewf_fail(e_ == cudaErrorMemoryAllocation ? EWF_ERR_NOMEM : EWF_ERR_CUDA,          \
+                            "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);     \
+    } while (0)
+
+extern "C" const char *ewf_last_error(void) { return g_err; }
+
+extern "C" int ewf_abi_version(void) { return EWF_ABI_VERSION; }
+
+extern "C" const char *ewf_strerror(int s)
+{
+    switch (s) {
+    case EWF_OK: return "ok";
+    case EWF_ERR_ARG: return "invalid argument";
+    case EWF_ERR_CUDA: return "CUDA error";
+    case EWF_ERR_NOMEM: return "out of memory";
+    case EWF_ERR_IO: return "file I/O error";
+    case EWF_ERR_STATE: return "call out of order";
+    case EWF_ERR_CFL: return "time step above the CFL limit";
+    case EWF_ERR_NONFINITE: return "non-finite values in the receiver traces";
+    case EWF_ERR_UNSUPPORTED: return "unsupported configuration";
+    case EWF_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+    }
+}
+
+extern "C" void ewf_params_default(ewf_params *p)
+{
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->model = EWF_MODEL_ISO;
+    p->precision = EWF_PREC_F32;
+    p->damping = EWF_DAMP_PML1D;
+    p->src_order = EWF_SRC_BEFORE_BC1;
+    p->check_finite = 1;
+    p->dx = p->dy = p->dz = 1.0;
+    p->dt = 1.0;
+}
+
+// ------------------------------------------------------------------------------------------
+// geometry helpers
+// ------------------------------------------------------------------------------------------
+// Extents (reference layout) of a field id; returns false for unknown ids.
+bool ewf_field_extent(const ewf_params &p, int id, int *ex, int *ey, int *ez)
+{
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    int x = nx, y = ny, z = nz;
+    switch (id) {
+    case EWF_F_VX: case EWF_M_BX: x = nx + 1; break;
+    case EWF_F_VY: case EWF_M_BY: y = ny + 1; break;
+    case EWF_F_VZ: case EWF_M_BZ: z = nz + 1; break;
+    case EWF_F_SXX: case EWF_F_SYY: case EWF_F_SZZ: break;
+    case EWF_F_SXY: case EWF_M_C66XY: x = nx + 1; y = ny + 1; break;
+    case EWF_F_SXZ: case EWF_M_C55XZ: x = nx + 1; z = nz + 1; break;
+    case EWF_F_SYZ: case EWF_M_C44YZ: y = ny + 1; z = nz + 1; break;
+    case EWF_M_C11: case EWF_M_C12: break;
+    case EWF_M_C22: case EWF_M_C33: case EWF_M_C13: case EWF_M_C23:
+        if (p.model != EWF_MODEL_ORTHO) return false;
+        break;
+    case EWF_D_WX: x = nx + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
+    case EWF_D_WY: x = ny + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
+    case EWF_D_WZ: x = nz + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
+    case EWF_D_W3D: break;
+    default: return false;
+    }
+    if ((id == EWF_M_C66XY || id == EWF_M_C55XZ || id == EWF_M_C44YZ || id == EWF_M_BX || id == EWF_M_BY ||
+         id == EWF_M_BZ) && p.model != EWF_MODEL_ORTHO)
+        return false;
+    if ((id == EWF_D_WX || id == EWF_D_WY || id == EWF_D_WZ) && p.damping == EWF_DAMP_W3D) return false;
+    if (id == EWF_D_W3D && p.damping != EWF_DAMP_W3D) return false;
+    *ex = x; *ey = y; *ez = z;
+    return true;
+}
+
+// material slot of a field id (index into m[]), -1 if not a material
+static int material_slot(int model, int id)
+{
+    if (model == EWF_MODEL_ISO) {
+        if (id == EWF_M_C11) return 0;
+        if (id == EWF_M_C12) return 1;
+        return -1;
+    }
+    switch (id) {
+    case EWF_M_C11: return 0;
+    case EWF_M_C22: return 1;
+    case EWF_M_C33: return 2;
+    case EWF_M_C12: return 3;
+    case EWF_M_C13: return 4;
+    case EWF_M_C23: return 5;
+    case EWF_M_C66XY: return 6;
+    case EWF_M_C55XZ: return 7;
+    case EWF_M_C44YZ: return 8;
+    case EWF_M_BX: return 9;
+    case EWF_M_BY: return 10;
+    case EWF_M_BZ: return 11;
+    default: return -1;
+    }
+}
+
+static int n_materials(int model) { return model == EWF_MODEL_ISO ? 2 : 12; }
+
+// ------------------------------------------------------------------------------------------
+// handle
+// ------------------------------------------------------------------------------------------
+struct ewf_handle {
+    ewf_params p;
+    std::string workdir;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t esz = 4;
+    int hx = 0, sx = 0;
+    long long sy = 0;
+    size_t box_elems = 0;
+    long long base_off = 0;  // element offset of (0,0,0) inside an allocation
+    void *f_alloc[9] = {};
+    void *comp_alloc[3] = {};
+    void *m_alloc[12] = {};
+    bool m_set[12] = {};
+    void *w1[3] = {};
+    bool w_set[4] = {};
+    void *w3_alloc = nullptr;
+    double *d_stf = nullptr;
+    size_t nstf = 0;
+    SrcEntry *d_src = nullptr;
+    int nsrc = 0;
+    std::vector<SrcEntry> h_src;
+    long long *d_rec_off = nullptr;
+    int *d_rec_comp = nullptr;
+    int nrec = 0;
+    std::vector<int32_t> h_rec;  // n*4 (i,j,k,comp)
+    double *d_traces = nullptr;
+    int *d_it = nullptr;
+    int it = 0;
+    void *d_stage = nullptr;
+    size_t stage_bytes = 0;
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    bool graph_dirty = true;
+    float last_ms = 0.f;
+    int kchunk = 32;
+};
+
+static void *boxptr(const ewf_handle *h, void *alloc)
+{
+    return alloc ? (void *)((char *)alloc + h->base_off * (long long)h->esz) : nullptr;
+}
+
+template <typename T>
+static StepArgs<T> make_args(const ewf_handle *h)
+{
+    StepArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    for (int q = 0; q < 9; ++q) a.f[q] = (T *)boxptr(h, h->f_alloc[q]);
+    for (int q = 0; q < 3; ++q) a.comp[q] = (T *)boxptr(h, h->comp_alloc[q]);
+    for (int q = 0; q < 12; ++q) a.m[q] = (const T *)boxptr(h, h->m_alloc[q]);
+    for (int q = 0; q < 3; ++q) a.w1[q] = (const T *)h->w1[q];
+    a.w3 = (const T *)boxptr(h, h->w3_alloc);
+    a.sy = h->sy;
+    a.sx = h->sx;
+    a.nx = h->p.nx;
+    a.ny = h->p.ny;
+    a.nz = h->p.nz;
+    a.bc1_rows = std::min(h->p.nx, h->p.ny + std::max(0, h->p.over_y));
+    if (a.bc1_rows > h->p.ny) a.bc1_rows = h->p.ny;
+    a.kchunk = h->kchunk;
+    // scalar parameters are rounded to T exactly as the reference passes them (const DAT args)
+    a.dt = (T)h->p.dt;
+    a.dx = (T)h->p.dx;
+    a.dy = (T)h->p.dy;
+    a.dz = (T)h->p.dz;
+    a.rdt = (T)1.0 / a.dt;
+    a.rdx = (T)1.0 / a.dx;
+    a.rdy = (T)1.0 / a.dy;
+    a.rdz = (T)1.0 / a.dz;
+    a.c66 = (T)h->p.c66;
+    a.bx = (T)h->p.bx;
+    a.by = (T)h->p.by;
+    a.bz = (T)h->p.bz;
+    a.third = (T)1.0 / (T)3.0;
+    return a;
+}
+
+static int dev_zero(ewf_handle *h, void *alloc)
+{
+    if (alloc) CK(cudaMemsetAsync(alloc, 0, h->box_elems * h->esz, h->stream));
+    return EWF_OK;
+}
+
+static int alloc_box(ewf_handle *h, void **out)
+{
+    CK(cudaMalloc(out, h->box_elems * h->esz));
+    CK(cudaMemsetAsync(*out, 0, h->box_elems * h->esz, h->stream));
+    return EWF_OK;
+}
+
+extern "C" void ewf_destroy(ewf_handle *h)
+{
+    if (!h) return;
+    int cur = -1;
+    cudaGetDevice(&cur);
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    for (auto &x : h->f_alloc) cudaFree(x);
+    for (auto &x : h->comp_alloc) cudaFree(x);
+    for (auto &x : h->m_alloc) cudaFree(x);
+    for (auto &x : h->w1) cudaFree(x);
+    cudaFree(h->w3_alloc);
+    cudaFree(h->d_stf);
+    cudaFree(h->d_src);
+    cudaFree(h->d_rec_off);
+    cudaFree(h->d_rec_comp);
+    cudaFree(h->d_traces);
+    cudaFree(h->d_it);
+    cudaFree(h->d_stage);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    if (cur >= 0) cudaSetDevice(cur);
+    delete h;
+}
+
+static int validate_params(const ewf_params *p)
+{
+    if (!p) return ewf_fail(EWF_ERR_ARG, "params is NULL");
+    if (p->nx < 4 || p->ny < 4 || p->nz < 4)
+        return ewf_fail(EWF_ERR_ARG, "grid %dx%dx%d: every extent must be >= 4", p->nx, p->ny, p->nz);
+    if ((long long)p->nx * p->ny * p->nz > (1LL << 36)) return ewf_fail(EWF_ERR_ARG, "grid too large");
+    if (p->nt < 1) return ewf_fail(EWF_ERR_ARG, "nt must be >= 1 (got %d)", p->nt);
+    if (p->model != EWF_MODEL_ISO && p->model != EWF_MODEL_ORTHO) return ewf_fail(EWF_ERR_ARG, "unknown model %d", p->model);
+    if (p->precision < EWF_PREC_F32 || p->precision > EWF_PREC_F64) return ewf_fail(EWF_ERR_ARG, "unknown precision %d", p->precision);
+    if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles (damping 0)");
+    if (p->model == EWF_MODEL_ORTHO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "the orthorhombic scheme uses a 3-D or separable weight field (damping 1 or 2)");
+    if (p->src_order != EWF_SRC_BEFORE_BC1 && p->src_order != EWF_SRC_AFTER_BC1)
+        return ewf_fail(EWF_ERR_ARG, "unknown src_order %d", p->src_order);
+    if (p->over_y < 0) return ewf_fail(EWF_ERR_ARG, "over_y must be >= 0");
+    if (p->nx > p->ny && p->over_y > 0)
+        return ewf_fail(EWF_ERR_UNSUPPORTED,
+                        "nx > ny with over_y > 0: the reference free-surface kernel writes rows past ny into the next "
+                        "plane while other threads read it (a race); no defined result to reproduce");
+    if (!(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->dt > 0)) return ewf_fail(EWF_ERR_ARG, "dx, dy, dz, dt must be > 0");
+    if (p->kchunk != 0 && p->kchunk < 4) return ewf_fail(EWF_ERR_ARG, "kchunk must be 0 or >= 4");
+    return EWF_OK;
+}
+
+extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
+{
+    if (!out) return ewf_fail(EWF_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int st = validate_params(p);
+    if (st) return st;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return ewf_fail(EWF_ERR_NODEVICE, "no CUDA device visible");
+    }
+    ewf_handle *h = new (std::nothrow) ewf_handle();
+    if (!h) return ewf_fail(EWF_ERR_NOMEM, "host allocation");
+    h->p = *p;
+    h->workdir = p->workdir ? p->workdir : ".";
+    h->p.workdir = nullptr;
+    cudaGetDevice(&h->device);
+    h->esz = (p->precision == EWF_PREC_F64) ? 8 : 4;
+    h->hx = (int)(128 / h->esz);
+    const int nx = p->nx, ny = p->ny, nz = p->nz;
+    h->sx = h->hx + ((nx + 2 + 31) / 32) * 32;
+    const long long py = ny + 3, pz = nz + 3;
+    h->sy = (long long)h->sx * py;
+    h->box_elems = (size_t)h->sy * pz;
+    h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
+    h->kchunk = p->kchunk > 0 ? p->kchunk : (nz >= 256 ? 32 : 16);
+    h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
+
+#define CKH(call)                                                                                    \
+    do {                                                                                             \
+        int s_ = (call);                                                                             \
+        if (s_) { ewf_destroy(h); return s_; }                                                       \
+    } while (0)
+#define CKC(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) {                                                                     \
+            int s_ = ewf_fail(e_ == cudaErrorMemoryAllocation ? EWF_ERR_NOMEM : EWF_ERR_CUDA,         \
+                              "%s: %s", #call, cudaGetErrorString(e_));                              \
+            ewf_destroy(h);                                                                          \
+            return s_;                                                                               \
+        }                                                                                            \
+    } while (0)
+
+    CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CKC(cudaEventCreate(&h->ev0));
+    CKC(cudaEventCreate(&h->ev1));
+    for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
+    if (p->precision == EWF_PREC_F32_KAHAN)
+        for (int q = 0; q < 3; ++q) CKH(alloc_box(h, &h->comp_alloc[q]));
+    for (int q = 0; q < n_materials(p->model); ++q) CKH(alloc_box(h, &h->m_alloc[q]));
+    if (p->damping == EWF_DAMP_W3D) {
+        CKH(alloc_box(h, &h->w3_alloc));
+    } else {
+        const int n1[3] = {nx + 1, ny + 1, nz + 1};
+        for (int q = 0; q < 3; ++q) {
+            CKC(cudaMalloc(&h->w1[q], (size_t)(n1[q] + 1) * h->esz));
+            CKC(cudaMemsetAsync(h->w1[q], 0, (size_t)(n1[q] + 1) * h->esz, h->stream));
+        }
+    }
+    CKC(cudaMalloc(&h->d_it, sizeof(int)));
+    CKC(cudaMemsetAsync(h->d_it, 0, sizeof(int), h->stream));
+    // staging buffer for host transfers in the reference layout (largest field, FP64)
+    h->stage_bytes = (size_t)(nx + 1) * (ny + 1) * (nz + 1) * 8;
+    CKC(cudaMalloc(&h->d_stage, h->stage_bytes));
+    CKC(cudaStreamSynchronize(h->stream));
+#undef CKH
+#undef CKC
+    *out = h;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_params(const ewf_handle *h, ewf_params *out)
+{
+    if (!h || !out) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *out = h->p;
+    out->workdir = h->workdir.c_str();
+    return EWF_OK;
+}
+
+const char *ewf_workdir(const ewf_handle *h) { return h->workdir.c_str(); }
+int ewf_nrec(const ewf_handle *h) { return h->nrec; }
+int ewf_esz(const ewf_handle *h) { return (int)h->esz; }
+const double *ewf_stf_host_copy(const ewf_handle *h, std::vector<double> &out)
+{
+    out.resize(h->nstf);
+    if (h->nstf) cudaMemcpy(out.data(), h->d_stf, h->nstf * sizeof(double), cudaMemcpyDeviceToHost);
+    return out.data();
+}
+
+extern "C" size_t ewf_field_size(const ewf_handle *h, int32_t field)
+{
+    if (!h) return 0;
+    int ex, ey, ez;
+    if (!ewf_field_extent(h->p, field, &ex, &ey, &ez)) return 0;
+    return (size_t)ex * ey * ez;
+}
+
+// device pointer (box base or 1-D array) of a field id
+static void *field_dev(ewf_handle *h, int id, bool *is_box)
+{
+    *is_box = true;
+    if (id >= EWF_F_VX && id <= EWF_F_SYZ) return boxptr(h, h->f_alloc[id]);
+    const int ms = material_slot(h->p.model, id);
+    if (ms >= 0) return boxptr(h, h->m_alloc[ms]);
+    if (id == EWF_D_W3D) return boxptr(h, h->w3_alloc);
+    if (id >= EWF_D_WX && id <= EWF_D_WZ) {
+        *is_box = false;
+        return h->w1[id - EWF_D_WX];
+    }
+    return nullptr;
+}
+
+static unsigned pack_blocks(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16); }
+
+extern "C" int ewf_set_field(ewf_handle *h, int32_t field, const void *host, size_t n, int32_t dtype_bytes)
+{
+    if (!h || !host) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    if (dtype_bytes != 4 && dtype_bytes != 8) return ewf_fail(EWF_ERR_ARG, "dtype_bytes must be 4 or 8");
+    int ex, ey, ez;
+    if (!ewf_field_extent(h->p, field, &ex, &ey, &ez))
+        return ewf_fail(EWF_ERR_ARG, "field %d does not exist for this model/damping", field);
+    const size_t need = (size_t)ex * ey * ez;
+    if (n != need) return ewf_fail(EWF_ERR_ARG, "field %d: %zu elements given, %zu expected", field, n, need);
+    bool is_box;
+    void *dst = field_dev(h, field, &is_box);
+    if (!dst) return ewf_fail(EWF_ERR_STATE, "field %d has no storage", field);
+    CK(cudaMemcpyAsync(h->d_stage, host, n * dtype_bytes, cudaMemcpyHostToDevice, h->stream));
+    const int sx = is_box ? h->sx : 0;
+    const long long sy = is_box ? h->sy : 0;
+    const unsigned nb = pack_blocks(n);
+    if (h->esz == 4) {
+        if (dtype_bytes == 4) k_pack<float, float><<<nb, 256, 0, h->stream>>>((float *)dst, (const float *)h->d_stage, ex, ey, ez, sx, sy);
+        else k_pack<float, double><<<nb, 256, 0, h->stream>>>((float *)dst, (const double *)h->d_stage, ex, ey, ez, sx, sy);
+    } else {
+        if (dtype_bytes == 4) k_pack<double, float><<<nb, 256, 0, h->stream>>>((double *)dst, (const float *)h->d_stage, ex, ey, ez, sx, sy);
+        else k_pack<double, double><<<nb, 256, 0, h->stream>>>((double *)dst, (const double *)h->d_stage, ex, ey, ez, sx, sy);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    const int ms = material_slot(h->p.model, field);
+    if (ms >= 0) h->m_set[ms] = true;
+    if (field >= EWF_D_WX && field <= EWF_D_W3D) h->w_set[field - EWF_D_WX] = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_field(ewf_handle *h, int32_t field, void *host, size_t n, int32_t dtype_bytes)
+{
+    if (!h || !host) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    if (dtype_bytes != 4 && dtype_bytes != 8) return ewf_fail(EWF_ERR_ARG, "dtype_bytes must be 4 or 8");
+    int ex, ey, ez;
+    if (!ewf_field_extent(h->p, field, &ex, &ey, &ez))
+        return ewf_fail(EWF_ERR_ARG, "field %d does not exist for this model/damping", field);
+    const size_t need = (size_t)ex * ey * ez;
+    if (n != need) return ewf_fail(EWF_ERR_ARG, "field %d: %zu elements given, %zu expected", field, n, need);
+    bool is_box;
+    void *src = field_dev(h, field, &is_box);
+    if (!src) return ewf_fail(EWF_ERR_STATE, "field %d has no storage", field);
+    const int sx = is_box ? h->sx : 0;
+    const long long sy = is_box ? h->sy : 0;
+    const unsigned nb = pack_blocks(n);
+    if (h->esz == 4) {
+        if (dtype_bytes == 4) k_unpack<float, float><<<nb, 256, 0, h->stream>>>((float *)h->d_stage, (const float *)src, ex, ey, ez, sx, sy);
+        else k_unpack<double, float><<<nb, 256, 0, h->stream>>>((double *)h->d_stage, (const float *)src, ex, ey, ez, sx, sy);
+    } else {
+        if (dtype_bytes == 4) k_unpack<float, double><<<nb, 256, 0, h->stream>>>((float *)h->d_stage, (const double *)src, ex, ey, ez, sx, sy);
+        else k_unpack<double, double><<<nb, 256, 0, h->stream>>>((double *)h->d_stage, (const double *)src, ex, ey, ez, sx, sy);
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, h->d_stage, n * dtype_bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_stf(ewf_handle *h, const double *stf, size_t n)
+{
+    if (!h || (!stf && n)) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    if (n < (size_t)h->p.nt) return ewf_fail(EWF_ERR_ARG, "Src has %zu samples, nt = %d", n, h->p.nt);
+    if (n != h->nstf) {
+        CK(cudaStreamSynchronize(h->stream));
+        cudaFree(h->d_stf);
+        h->d_stf = nullptr;
+        h->nstf = 0;
+        CK(cudaMalloc(&h->d_stf, n * sizeof(double)));
+        h->nstf = n;
+        h->graph_dirty = true;
+    }
+    CK(cudaMemcpyAsync(h->d_stf, stf, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_sources(ewf_handle *h, int32_t n, const int32_t *cijk, const double *coef)
+{
+    if (!h || n < 0 || (n > 0 && (!cijk || !coef))) return ewf_fail(EWF_ERR_ARG, "bad source list");
+    std::vector<SrcEntry> v((size_t)n);
+    for (int e = 0; e < n; ++e) {
+        const int c = cijk[4 * e], i = cijk[4 * e + 1], j = cijk[4 * e + 2], k = cijk[4 * e + 3];
+        if (c < EWF_F_SXX || c > EWF_F_SYZ) return ewf_fail(EWF_ERR_ARG, "source %d: component %d is not a stress field", e, c);
+        int ex, ey, ez;
+        ewf_field_extent(h->p, c, &ex, &ey, &ez);
+        if (i < 0 || j < 0 || k < 0 || i >= ex || j >= ey || k >= ez)
+            return ewf_fail(EWF_ERR_ARG, "source %d: cell (%d,%d,%d) outside field %d (%dx%dx%d)", e, i, j, k, c, ex, ey, ez);
+        v[e] = SrcEntry{c, i, j, k, coef[e]};
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    if (n > h->nsrc || !h->d_src) {
+        cudaFree(h->d_src);
+        h->d_src = nullptr;
+        if (n > 0) CK(cudaMalloc(&h->d_src, (size_t)n * sizeof(SrcEntry)));
+    }
+    if (n > 0) CK(cudaMemcpy(h->d_src, v.data(), (size_t)n * sizeof(SrcEntry), cudaMemcpyHostToDevice));
+    h->h_src = v;
+    h->nsrc = n;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_moment_tensor(ewf_handle *h, const double mt[6], int32_t xs, int32_t ys, int32_t zs, int32_t stencil)
+{
+    if (!h || !mt) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    // component order of mt: xx yy zz xy xz yz
+    int32_t cijk[24];
+    double coef[6];
+    int n = 0;
+    auto add = [&](int comp, int di, int dj, int dk, double c) {
+        cijk[4 * n] = comp; cijk[4 * n + 1] = xs + di; cijk[4 * n + 2] = ys + dj; cijk[4 * n + 3] = zs + dk;
+        coef[n++] = c;
+    };
+    if (stencil == 0) {
+        // OK4:336-342: normals at (xs+1,ys+1,zs+1), yz at (xs+2,ys+2), xz and xy at (xs+3,ys+3)
+        add(EWF_F_SXX, 1, 1, 1, mt[0]);
+        add(EWF_F_SYY, 1, 1, 1, mt[1]);
+        add(EWF_F_SZZ, 1, 1, 1, mt[2]);
+        add(EWF_F_SYZ, 2, 2, 1, mt[5]);
+        add(EWF_F_SXZ, 3, 3, 1, mt[4]);
+        add(EWF_F_SXY, 3, 3, 1, mt[3]);
+    } else if (stencil == 1) {
+        // ANISO:233-247: normals at (xs+1,ys+1), xy at (xs+2,ys+2), yz at (xs+3,ys+2), xz at (xs-1,ys+1)
+        add(EWF_F_SXX, 1, 1, 1, mt[0]);
+        add(EWF_F_SYY, 1, 1, 1, mt[1]);
+        add(EWF_F_SZZ, 1, 1, 1, mt[2]);
+        add(EWF_F_SXY, 2, 2, 1, mt[3]);
+        add(EWF_F_SYZ, 3, 2, 1, mt[5]);
+        add(EWF_F_SXZ, -1, 1, 1, mt[4]);
+    } else {
+        return ewf_fail(EWF_ERR_ARG, "stencil must be 0 (OK4) or 1 (ANISO)");
+    }
+    return ewf_set_sources(h, n, cijk, coef);
+}
+
+extern "C" int ewf_set_receivers(ewf_handle *h, int32_t n, const int32_t *ijkc)
+{
+    if (!h || n < 0 || (n > 0 && !ijkc)) return ewf_fail(EWF_ERR_ARG, "bad receiver list");
+    std::vector<long long> off((size_t)n);
+    std::vector<int> comp((size_t)n);
+    for (int r = 0; r < n; ++r) {
+        const int i = ijkc[4 * r], j = ijkc[4 * r + 1], k = ijkc[4 * r + 2], c = ijkc[4 * r + 3];
+        if (c < EWF_F_VX || c > EWF_F_SYZ) return ewf_fail(EWF_ERR_ARG, "receiver %d: field %d is not a state field", r, c);
+        int ex, ey, ez;
+        ewf_field_extent(h->p, c, &ex, &ey, &ez);
+        if (i < 0 || j < 0 || k < 0 || i >= ex || j >= ey || k >= ez)
+            return ewf_fail(EWF_ERR_ARG, "receiver %d: cell (%d,%d,%d) outside field %d", r, i, j, k, c);
+        off[r] = (long long)i + (long long)j * h->sx + (long long)k * h->sy;
+        comp[r] = c;
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    cudaFree(h->d_rec_off);
+    cudaFree(h->d_rec_comp);
+    cudaFree(h->d_traces);
+    h->d_rec_off = nullptr;
+    h->d_rec_comp = nullptr;
+    h->d_traces = nullptr;
+    h->nrec = 0;
+    if (n > 0) {
+        CK(cudaMalloc(&h->d_rec_off, (size_t)n * sizeof(long long)));
+        CK(cudaMalloc(&h->d_rec_comp, (size_t)n * sizeof(int)));
+        CK(cudaMalloc(&h->d_traces, (size_t)n * h->p.nt * sizeof(double)));
+        CK(cudaMemcpy(h->d_rec_off, off.data(), (size_t)n * sizeof(long long), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_rec_comp, comp.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemset(h->d_traces, 0, (size_t)n * h->p.nt * sizeof(double)));
+    }
+    h->nrec = n;
+    h->h_rec.assign(ijkc, ijkc + 4 * (size_t)n);
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_receiver_count(const ewf_handle *h, int32_t *n)
+{
+    if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *n = h->nrec;
+    return EWF_OK;
+}
+
+extern "C" int ewf_reset(ewf_handle *h)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    for (auto x : h->f_alloc) { int s = dev_zero(h, x); if (s) return s; }
+    for (auto x : h->comp_alloc) { int s = dev_zero(h, x); if (s) return s; }
+    if (h->d_traces) CK(cudaMemsetAsync(h->d_traces, 0, (size_t)h->nrec * h->p.nt * sizeof(double), h->stream));
+    CK(cudaMemsetAsync(h->d_it, 0, sizeof(int), h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->it = 0;
+    return EWF_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// the time step
+// ------------------------------------------------------------------------------------------
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t *ev)
+{
+    const dim3 blk(TX, TY);
+    const dim3 grd((h->p.nx + TX - 1) / TX, (h->p.ny + TY - 1) / TY, (h->p.nz + a.kchunk - 1) / a.kchunk);
+    if (ev) cudaEventRecord(ev[0], h->stream);
+    k_stress<T, MODEL, DAMP><<<grd, blk, 0, h->stream>>>(a);
+    if (ev) cudaEventRecord(ev[1], h->stream);
+    if (h->nsrc > 0)
+        k_inject<T><<<1, 32, 0, h->stream>>>(a, h->d_src, h->nsrc, h->d_stf, (int)h->nstf, h->d_it, h->p.src_order);
+    if (ev) cudaEventRecord(ev[2], h->stream);
+    k_velocity<T, MODEL, DAMP, KAHAN><<<grd, blk, 0, h->stream>>>(a);
+    if (ev) cudaEventRecord(ev[3], h->stream);
+    k_record<T><<<1, 256, 0, h->stream>>>(a, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    if (ev) cudaEventRecord(ev[4], h->stream);
+}
+
+typedef void (*step_fn)(const ewf_handle *, cudaEvent_t *);
+
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+static void step_entry(const ewf_handle *h, cudaEvent_t *ev)
+{
+    const StepArgs<T> a = make_args<T>(h);
+    launch_step_t<T, MODEL, DAMP, KAHAN>(h, a, ev);
+}
+
+static step_fn pick_step(const ewf_params &p)
+{
+    const bool iso = p.model == EWF_MODEL_ISO;
+    const bool w3 = p.damping == EWF_DAMP_W3D;
+    switch (p.precision) {
+    case EWF_PREC_F32:
+        if (iso) return step_entry<float, MODEL_ISO, DAMP_PML1D, false>;
+        return w3 ? step_entry<float, MODEL_ORTHO, DAMP_W3D, false> : step_entry<float, MODEL_ORTHO, DAMP_SEP, false>;
+    case EWF_PREC_F32_KAHAN:
+        if (iso) return step_entry<float, MODEL_ISO, DAMP_PML1D, true>;
+        return w3 ? step_entry<float, MODEL_ORTHO, DAMP_W3D, true> : step_entry<float, MODEL_ORTHO, DAMP_SEP, true>;
+    default:
+        if (iso) return step_entry<double, MODEL_ISO, DAMP_PML1D, false>;
+        return w3 ? step_entry<double, MODEL_ORTHO, DAMP_W3D, false> : step_entry<double, MODEL_ORTHO, DAMP_SEP, false>;
+    }
+}
+
+static int inputs_ready(const ewf_handle *h)
+{
+    for (int q = 0; q < n_materials(h->p.model); ++q)
+        if (!h->m_set[q]) return ewf_fail(EWF_ERR_STATE, "material slot %d not set", q);
+    if (h->p.damping == EWF_DAMP_W3D) {
+        if (!h->w_set[3]) return ewf_fail(EWF_ERR_STATE, "3-D weights not set");
+    } else {
+        for (int q = 0; q < 3; ++q)
+            if (!h->w_set[q]) return ewf_fail(EWF_ERR_STATE, "damping profile %d not set", q);
+    }
+    if (h->nsrc > 0 && !h->d_stf) return ewf_fail(EWF_ERR_STATE, "sources set but no source time function");
+    return EWF_OK;
+}
+
+static int build_graph(ewf_handle *h, step_fn fn)
+{
+    if (h->gexec) {
+        cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr);
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return ewf_fail(EWF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        h->gexec = nullptr;
+        return ewf_fail(EWF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+    }
+    h->graph_dirty = false;
+    return EWF_OK;
+}
+
+extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (nsteps < 0) return ewf_fail(EWF_ERR_ARG, "nsteps < 0");
+    int st = inputs_ready(h);
+    if (st) return st;
+    if (h->it + nsteps > h->p.nt)
+        return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
+    if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf)
+        return ewf_fail(EWF_ERR_ARG, "source time function has %zu samples, need %d", h->nstf, h->it + nsteps);
+    const step_fn fn = pick_step(h->p);
+    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps;
+    if (use_graph && (h->graph_dirty || !h->gexec)) {
+        st = build_graph(h, fn);
+        if (st) return st;
+    }
+    CK(cudaEventRecord(h->ev0, h->stream));
+    int done = 0;
+    if (use_graph) {
+        for (; done + h->gsteps <= nsteps; done += h->gsteps) {
+            CK(cudaGraphLaunch(h->gexec, h->stream));
+            if (h->p.nout > 0 && ((h->it + done) / h->p.nout) != ((h->it + done + h->gsteps) / h->p.nout)) {
+                printf("it=%05d > ", h->it + done + h->gsteps);
+                fflush(stdout);
+            }
+        }
+    }
+    for (; done < nsteps; ++done) fn(h, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
+    h->it += nsteps;
+    if (h->p.check_finite && h->nrec > 0 && nsteps > 0) {
+        std::vector<double> tr((size_t)h->nrec * h->p.nt);
+        CK(cudaMemcpy(tr.data(), h->d_traces, tr.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int r = 0; r < h->nrec; ++r)
+            for (int t = h->it - nsteps; t < h->it; ++t)
+                if (!std::isfinite(tr[(size_t)r * h->p.nt + t]))
+                    return ewf_fail(EWF_ERR_NONFINITE, "receiver %d has a non-finite sample at step %d", r, t);
+    }
+    return EWF_OK;
+}
+
+extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
+{
+    if (!h || !out_ms || nsteps < 1) return ewf_fail(EWF_ERR_ARG, "bad argument");
+    int st = inputs_ready(h);
+    if (st) return st;
+    if (h->it + nsteps > h->p.nt) return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
+    if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf) return ewf_fail(EWF_ERR_ARG, "source time function too short");
+    const step_fn fn = pick_step(h->p);
+    cudaEvent_t ev[5] = {};
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    double acc[4] = {0, 0, 0, 0};
+    int err = EWF_OK;
+    for (int s = 0; s < nsteps && !err; ++s) {
+        fn(h, ev);
+        if (cudaEventSynchronize(ev[4]) != cudaSuccess) { err = ewf_fail(EWF_ERR_CUDA, "kernel timing: %s", cudaGetErrorString(cudaGetLastError())); break; }
+        for (int q = 0; q < 4; ++q) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+            acc[q] += ms;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (err) return err;
+    CK(cudaGetLastError());
+    h->it += nsteps;
+    for (int q = 0; q < 4; ++q) out_ms[q] = acc[q] / nsteps;
+    return EWF_OK;
+}
+
+extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
+{
+    if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *n = 3 + (h->nsrc > 0 ? 1 : 0);
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_step(const ewf_handle *h, int32_t *it)
+{
+    if (!h || !it) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *it = h->it;
+    return EWF_OK;
+}
+
+extern "C" int ewf_last_run_ms(const ewf_handle *h, double *ms)
+{
+    if (!h || !ms) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *ms = h->last_ms;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_seismograms(ewf_handle *h, double *out, size_t n)
+{
+    if (!h || (!out && n)) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    const size_t need = (size_t)h->nrec * h->p.nt;
+    if (n != need) return ewf_fail(EWF_ERR_ARG, "%zu samples given, %zu expected (n_rec x nt)", n, need);
+    if (need) CK(cudaMemcpyAsync(out, h->d_traces, need * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return EWF_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// checkpoint / restore: header, 9 state fields (+3 compensation), traces -- reference layout
+// ------------------------------------------------------------------------------------------
+struct CkptHeader {
+    char magic[8];
+    int32_t version, nx, ny, nz, nt, model, precision, damping, it, nrec, ncomp, pad;
+};
+
+extern "C" int ewf_checkpoint(ewf_handle *h, const char *path)
+{
+    if (!h || !path) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return ewf_fail(EWF_ERR_IO, "cannot open %s for writing", path);
+    CkptHeader hd;
+    memset(&hd, 0, sizeof(hd));
+    memcpy(hd.magic, "EWFCKPT1", 8);
+    hd.version = 1; hd.nx = h->p.nx; hd.ny = h->p.ny; hd.nz = h->p.nz; hd.nt = h->p.nt;
+    hd.model = h->p.model; hd.precision = h->p.precision; hd.damping = h->p.damping;
+    hd.it = h->it; hd.nrec = h->nrec; hd.ncomp = h->comp_alloc[0] ? 3 : 0;
+    int st = EWF_OK;
+    if (fwrite(&hd, sizeof(hd), 1, fp) != 1) st = ewf_fail(EWF_ERR_IO, "write %s", path);
+    std::vector<char> buf;
+    for (int q = 0; q < 9 + hd.ncomp && !st; ++q) {
+        const int id = q < 9 ? q : q - 9;
+        const size_t n = ewf_field_size(h, id);
+        buf.resize(n * h->esz);
+        if (q < 9) {
+            st = ewf_get_field(h, id, buf.data(), n, (int)h->esz);
+        } else {
+            // compensation arrays share Vx/Vy/Vz extents; unpack directly
+            int ex, ey, ez;
+            ewf_field_extent(h->p, id, &ex, &ey, &ez);
+            k_unpack<float, float><<<pack_blocks(n), 256, 0, h->stream>>>((float *)h->d_stage,
+                (const float *)boxptr(h, h->comp_alloc[id]), ex, ey, ez, h->sx, h->sy);
+            if (cudaMemcpyAsync(buf.data(), h->d_stage, n * 4, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+                cudaStreamSynchronize(h->stream) != cudaSuccess)
+                st = ewf_fail(EWF_ERR_CUDA, "checkpoint: compensation copy failed");
+        }
+        if (!st && fwrite(buf.data(), 1, buf.size(), fp) != buf.size()) st = ewf_fail(EWF_ERR_IO, "write %s", path);
+    }
+    if (!st && h->nrec) {
+        std::vector<double> tr((size_t)h->nrec * h->p.nt);
+        st = ewf_get_seismograms(h, tr.data(), tr.size());
+        if (!st && fwrite(tr.data(), sizeof(double), tr.size(), fp) != tr.size()) st = ewf_fail(EWF_ERR_IO, "write %s", path);
+    }
+    if (fclose(fp) != 0 && !st) st = ewf_fail(EWF_ERR_IO, "close %s", path);
+    return st;
+}
+
+extern "C" int ewf_restore(ewf_handle *h, const char *path)
+{
+    if (!h || !path) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return ewf_fail(EWF_ERR_IO, "cannot open %s", path);
+    CkptHeader hd;
+    int st = EWF_OK;
+    if (fread(&hd, sizeof(hd), 1, fp) != 1 || memcmp(hd.magic, "EWFCKPT1", 8) != 0) st = ewf_fail(EWF_ERR_IO, "%s is not a checkpoint", path);
+    if (!st && (hd.nx != h->p.nx || hd.ny != h->p.ny || hd.nz != h->p.nz || hd.nt != h->p.nt || hd.model != h->p.model ||
+                hd.precision != h->p.precision || hd.nrec != h->nrec))
+        st = ewf_fail(EWF_ERR_ARG, "checkpoint %s does not match this handle (grid/model/precision/receivers)", path);
+    std::vector<char> buf;
+    for (int q = 0; q < 9 + hd.ncomp && !st; ++q) {
+        const int id = q < 9 ? q : q - 9;
+        const size_t n = ewf_field_size(h, id);
+        buf.resize(n * h->esz);
+        if (fread(buf.data(), 1, buf.size(), fp) != buf.size()) { st = ewf_fail(EWF_ERR_IO, "short read %s", path); break; }
+        if (q < 9) {
+            st = ewf_set_field(h, id, buf.data(), n, (int)h->esz);
+        } else if (h->comp_alloc[id]) {
+            int ex, ey, ez;
+            ewf_field_extent(h->p, id, &ex, &ey, &ez);
+            if (cudaMemcpyAsync(h->d_stage, buf.data(), n * 4, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+                st = ewf_fail(EWF_ERR_CUDA, "restore: compensation copy failed");
+            k_pack<float, float><<<pack_blocks(n), 256, 0, h->stream>>>((float *)boxptr(h, h->comp_alloc[id]),
+                (const float *)h->d_stage, ex, ey, ez, h->sx, h->sy);
+            if (cudaStreamSynchronize(h->stream) != cudaSuccess) st = ewf_fail(EWF_ERR_CUDA, "restore: sync failed");
+        }
+    }
+    if (!st && h->nrec) {
+        std::vector<double> tr((size_t)h->nrec * h->p.nt);
+        if (fread(tr.data(), sizeof(double), tr.size(), fp) != tr.size()) st = ewf_fail(EWF_ERR_IO, "short read %s", path);
+        else if (cudaMemcpy(h->d_traces, tr.data(), tr.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+            st = ewf_fail(EWF_ERR_CUDA, "restore: trace copy failed");
+    }
+    fclose(fp);
+    if (!st) {
+        int it = hd.it;
+        if (cudaMemcpy(h->d_it, &it, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) return ewf_fail(EWF_ERR_CUDA, "restore: step copy");
+        h->it = it;
+    }
+    return st;
+}

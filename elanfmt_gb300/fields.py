@@ -1,0 +1,101 @@
+"""Constants of the C ABI (include/ewfd.h) and the reference's array geometry.
+
+Field extents follow the reference's allocations (FastWaveED_GPU3D_v1.cu:431-439 for the state,
+FastWaveED_GPU3D_v1_9kmst_ANISO.cu:411-456 for the orthorhombic model arrays); numpy arrays use
+shape (ez, ey, ex) in C order, i.e. x fastest as in the reference.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# ewf_model / ewf_precision / ewf_damping / ewf_src_order
+MODEL_ISO, MODEL_ORTHO = 0, 1
+PREC_F32, PREC_F32_KAHAN, PREC_F64 = 0, 1, 2
+DAMP_PML1D, DAMP_W3D, DAMP_SEPARABLE = 0, 1, 2
+SRC_BEFORE_BC1, SRC_AFTER_BC1 = 0, 1
+
+# state fields
+F_VX, F_VY, F_VZ, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ = range(9)
+STATE = tuple(range(9))
+STATE_NAMES = ("Vx", "Vy", "Vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")
+# materials
+M_C11, M_C12, M_C22, M_C33, M_C13, M_C23 = 16, 17, 18, 19, 20, 21
+M_C66XY, M_C55XZ, M_C44YZ, M_BX, M_BY, M_BZ = 22, 23, 24, 25, 26, 27
+ISO_MATERIALS = (M_C11, M_C12)
+ORTHO_MATERIALS = (M_C11, M_C22, M_C33, M_C12, M_C13, M_C23, M_C66XY, M_C55XZ, M_C44YZ, M_BX, M_BY, M_BZ)
+# damping
+D_WX, D_WY, D_WZ, D_W3D = 32, 33, 34, 35
+
+# status codes
+STATUS = {
+    0: "EWF_OK", -1: "EWF_ERR_ARG", -2: "EWF_ERR_CUDA", -3: "EWF_ERR_NOMEM", -4: "EWF_ERR_IO",
+    -5: "EWF_ERR_STATE", -6: "EWF_ERR_CFL", -7: "EWF_ERR_NONFINITE", -8: "EWF_ERR_UNSUPPORTED",
+    -9: "EWF_ERR_NODEVICE",
+}
+
+# legacy file names (FastWaveED_GPU3D_v1.cu:415-425, FastWaveED_GPU3D_v1_9kmst_ANISO.cu:411-456)
+LEGACY_FILES = {
+    M_C11: ("c11u_het.dat", "C11m.dat"), M_C12: ("c12u_het.dat", "C12m.dat"),
+    M_C22: (None, "C22m.dat"), M_C33: (None, "C33m.dat"), M_C13: (None, "C13m.dat"), M_C23: (None, "C23m.dat"),
+    M_C66XY: (None, "C66mxy.dat"), M_C55XZ: (None, "C55mxz.dat"), M_C44YZ: (None, "C44myz.dat"),
+    M_BX: (None, "vrho_x_11_hc.dat"), M_BY: (None, "vrho_y_11_hc.dat"), M_BZ: (None, "vrho_z_11_hc.dat"),
+    D_WX: ("weights_x.dat", None), D_WY: ("weights_y.dat", None), D_WZ: ("weights_z.dat", None),
+    D_W3D: (None, "weights.dat"),
+}
+
+
+def extent(fid: int, nx: int, ny: int, nz: int, damping: int = DAMP_PML1D) -> tuple[int, int, int]:
+    """(ex, ey, ez) of a field id in the reference layout."""
+    x, y, z = nx, ny, nz
+    if fid in (F_VX, M_BX):
+        x = nx + 1
+    elif fid in (F_VY, M_BY):
+        y = ny + 1
+    elif fid in (F_VZ, M_BZ):
+        z = nz + 1
+    elif fid in (F_SXY, M_C66XY):
+        x, y = nx + 1, ny + 1
+    elif fid in (F_SXZ, M_C55XZ):
+        x, z = nx + 1, nz + 1
+    elif fid in (F_SYZ, M_C44YZ):
+        y, z = ny + 1, nz + 1
+    elif fid in (D_WX, D_WY, D_WZ):
+        n = (nx, ny, nz)[fid - D_WX] + (1 if damping == DAMP_PML1D else 0)
+        return n, 1, 1
+    return x, y, z
+
+
+def shape(fid: int, nx: int, ny: int, nz: int, damping: int = DAMP_PML1D) -> tuple:
+    ex, ey, ez = extent(fid, nx, ny, nz, damping)
+    if fid in (D_WX, D_WY, D_WZ):
+        return (ex,)
+    return (ez, ey, ex)
+
+
+def mt_entries(mt, xs: int, ys: int, zs: int, stencil: int) -> tuple[np.ndarray, np.ndarray]:
+    """Point-source entries (comp, i, j, k) and coefficients of a moment tensor
+    (xx, yy, zz, xy, xz, yz) at the reference's injection stencil around (xs, ys, zs).
+
+    stencil 0 (FastWaveED_GPU3D_v1.cu:336-342): normals at (xs+1, ys+1, zs+1), yz at
+    (xs+2, ys+2), xz and xy at (xs+3, ys+3); stencil 1 (FastWaveED_GPU3D_v1_9kmst_ANISO.cu:233-247):
+    normals at (xs+1, ys+1), xy at (xs+2, ys+2), yz at (xs+3, ys+2), xz at (xs-1, ys+1); all at
+    zs+1.  Order of the entries is the reference's statement order."""
+    xx, yy, zz, xy, xz, yz = (float(v) for v in mt)
+    if stencil == 0:
+        e = [(F_SXX, 1, 1, xx), (F_SYY, 1, 1, yy), (F_SZZ, 1, 1, zz), (F_SYZ, 2, 2, yz), (F_SXZ, 3, 3, xz),
+             (F_SXY, 3, 3, xy)]
+    elif stencil == 1:
+        e = [(F_SXX, 1, 1, xx), (F_SYY, 1, 1, yy), (F_SZZ, 1, 1, zz), (F_SXY, 2, 2, xy), (F_SYZ, 3, 2, yz),
+             (F_SXZ, -1, 1, xz)]
+    else:
+        raise ValueError("stencil must be 0 or 1")
+    ent = np.array([(c, xs + di, ys + dj, zs + 1) for c, di, dj, _ in e], dtype=np.int32)
+    coef = np.array([v for *_, v in e], dtype=np.float64)
+    return ent, coef
+
+
+# the orthorhombic reference hard-codes its tensor (FastWaveED_GPU3D_v1_9kmst_ANISO.cu:233-247)
+ANISO_LEGACY_MT = tuple(float(np.float32(v)) for v in (-0.6282, 0.9437, 0.2439, 0.4455, -0.2709, -0.2362))
+# the four legacy traces Rec, Rec_x, Rec_y, Rec_y2 (FastWaveED_GPU3D_v1.cu:383-386; ANISO:263-266)
+OK4_LEGACY_RECEIVERS = ((504, 385, 1, F_VZ), (504, 385, 1, F_VX), (504, 388, 1, F_VY), (504, 387, 1, F_VY))
+ANISO_LEGACY_RECEIVERS = ((631, 257, 1, F_VZ), (631, 257, 1, F_VX), (631, 257, 1, F_VY), (631, 257, 1, F_VY))

@@ -1,0 +1,182 @@
+/*
+ * ewfd.h -- C ABI of the GB300 staggered-grid elastic FDTD solver (libewfd.so).
+ *
+ * Drop-in boundary for the reference's time loop.  The reference is one executable per
+ * scenario whose main() reads fixed-name float32 files from the current directory, runs the
+ * loop and writes "0_0_<name>.res" files (src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_OK4_final/
+ * FastWaveED_GPU3D_v1.cu:390-559, "OK4" below; src/FastWaveED_GPU3D_v1_9km_station_ANISO/
+ * FastWaveED_GPU3D_v1_9kmst_ANISO.cu:391-608, "ANISO" below).  Everything that executable
+ * fixes at compile time (-DNBX.. grid, nt, source cell, receiver cells, precision) is a
+ * runtime value here.
+ *
+ * Conventions
+ *   - Every function returns 0 (EWF_OK) or a negative ewf_status; none calls exit/abort.
+ *   - Host arrays use the reference layout: x fastest, idx = i + j*Px + k*Px*Py with the
+ *     array's own extents (Vx (nx+1,ny,nz), sxy (nx+1,ny+1,nz), ... OK4:431-439).
+ *   - Buffers passed in are owned by the caller and copied; the handle owns device memory.
+ *   - A handle is not thread-safe; it owns one CUDA stream on the device current at create.
+ */
+#ifndef EWFD_H
+#define EWFD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EWF_ABI_VERSION 1
+
+typedef enum ewf_status {
+    EWF_OK = 0,
+    EWF_ERR_ARG = -1,         /* invalid argument / size mismatch */
+    EWF_ERR_CUDA = -2,        /* CUDA runtime error (message in ewf_last_error) */
+    EWF_ERR_NOMEM = -3,       /* device or host allocation failed */
+    EWF_ERR_IO = -4,          /* legacy file missing, unreadable or of the wrong size */
+    EWF_ERR_STATE = -5,       /* call out of order (e.g. run before inputs are set) */
+    EWF_ERR_CFL = -6,         /* time step above the stability limit */
+    EWF_ERR_NONFINITE = -7,   /* NaN/Inf detected in the receiver traces */
+    EWF_ERR_UNSUPPORTED = -8, /* combination the reference leaves undefined / not built */
+    EWF_ERR_NODEVICE = -9     /* no CUDA device */
+} ewf_status;
+
+typedef enum ewf_model {
+    EWF_MODEL_ISO = 0,   /* isotropic: c11/c12 fields, scalar shear modulus and 1/rho (OK4:285-388) */
+    EWF_MODEL_ORTHO = 1  /* orthorhombic: 9 C_ij fields + staggered buoyancy (ANISO:287-389) */
+} ewf_model;
+
+typedef enum ewf_precision {
+    EWF_PREC_F32 = 0,       /* FP32, reference arithmetic (OK4:15-19) */
+    EWF_PREC_F32_KAHAN = 1, /* FP32 fields, compensated velocity time accumulation */
+    EWF_PREC_F64 = 2        /* FP64 (OK4:20-23 with USE_SINGLE_PRECISION off) */
+} ewf_precision;
+
+typedef enum ewf_damping {
+    EWF_DAMP_PML1D = 0,    /* 1-D profiles weights_x/y/z (n+1 each), OK4 usage (OK4:307-329, 361-375) */
+    EWF_DAMP_W3D = 1,      /* 3-D weights field (nx,ny,nz), ANISO usage (ANISO:312-386) */
+    EWF_DAMP_SEPARABLE = 2 /* ANISO usage with W[i,j,k] = (px[i]*py[j])*pz[k] formed on the fly */
+} ewf_damping;
+
+typedef enum ewf_src_order {
+    EWF_SRC_BEFORE_BC1 = 0, /* OK4: injection inside the stress kernel, BC1 after (OK4:336-342, 490) */
+    EWF_SRC_AFTER_BC1 = 1   /* ANISO: BC1, then the source kernel (ANISO:533-535) */
+} ewf_src_order;
+
+/* Field ids for ewf_set_field / ewf_get_field.  Extents are the reference's. */
+typedef enum ewf_field {
+    EWF_F_VX = 0, EWF_F_VY = 1, EWF_F_VZ = 2,          /* (nx+1,ny,nz) (nx,ny+1,nz) (nx,ny,nz+1) */
+    EWF_F_SXX = 3, EWF_F_SYY = 4, EWF_F_SZZ = 5,       /* (nx,ny,nz) */
+    EWF_F_SXY = 6, EWF_F_SXZ = 7, EWF_F_SYZ = 8,       /* (nx+1,ny+1,nz) (nx+1,ny,nz+1) (nx,ny+1,nz+1) */
+    /* materials, isotropic: c11u_het.dat, c12u_het.dat (OK4:415-418) */
+    EWF_M_C11 = 16, EWF_M_C12 = 17,
+    /* materials, orthorhombic (ANISO:411-447): C22m C33m C13m C23m, edge moduli, buoyancy */
+    EWF_M_C22 = 18, EWF_M_C33 = 19, EWF_M_C13 = 20, EWF_M_C23 = 21,
+    EWF_M_C66XY = 22, /* (nx+1,ny+1,nz) C66mxy.dat */
+    EWF_M_C55XZ = 23, /* (nx+1,ny,nz+1) C55mxz.dat */
+    EWF_M_C44YZ = 24, /* (nx,ny+1,nz+1) C44myz.dat */
+    EWF_M_BX = 25,    /* (nx+1,ny,nz) vrho_x_11_hc.dat */
+    EWF_M_BY = 26,    /* (nx,ny+1,nz) vrho_y_11_hc.dat */
+    EWF_M_BZ = 27,    /* (nx,ny,nz+1) vrho_z_11_hc.dat */
+    /* damping */
+    EWF_D_WX = 32, EWF_D_WY = 33, EWF_D_WZ = 34, /* PML1D: n+1 each (weights_x/y/z.dat); SEPARABLE: n each */
+    EWF_D_W3D = 35                               /* (nx,ny,nz) weights.dat */
+} ewf_field;
+
+typedef struct ewf_params {
+    int32_t nx, ny, nz;   /* grid; replaces nx = 64*NBX - OVERX etc. (OK4:39-41) */
+    int32_t nt;           /* time steps of a full run; replaces const nt (OK4:43) */
+    int32_t model;        /* ewf_model */
+    int32_t precision;    /* ewf_precision */
+    int32_t damping;      /* ewf_damping */
+    int32_t src_order;    /* ewf_src_order */
+    int32_t over_y;       /* legacy OVERY: BC1 rows are j < min(nx, ny + over_y) (OK4:279-281) */
+    int32_t nout;         /* progress line every nout steps (OK4:502-504); 0 = quiet */
+    int32_t kchunk;       /* planes per CTA of the z-marching kernels; 0 = autotuned/default */
+    int32_t graph_steps;  /* steps captured per CUDA graph; 0 = default, <0 = no graph */
+    int32_t check_finite; /* 1: ewf_run checks the receiver traces for NaN/Inf */
+    double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
+    double c66;            /* isotropic shear modulus pa2[7] (OK4:405) */
+    double bx, by, bz;     /* isotropic 1/rho pa3[0..2] (OK4:407) */
+    const char *workdir;   /* legacy *.dat inputs and *.res outputs (NULL = ".") */
+} ewf_params;
+
+typedef struct ewf_handle ewf_handle;
+
+int ewf_abi_version(void);
+const char *ewf_strerror(int status);
+/* Text of the last error on this thread (CUDA message, file name, ...). */
+const char *ewf_last_error(void);
+
+/* Defaults: FP32, iso, PML1D, before-BC1 order, over_y 0, graph on. */
+void ewf_params_default(ewf_params *p);
+
+/* Fills dx, dy, dz, dt, c66, bx, by, bz of p from p->workdir's pa1/pa2/pa3.dat (OK4:401-407)
+ * and, when p->nt is 0, nt from the length of Src.dat (the reference's compile-time nt, OK4:43). */
+int ewf_legacy_params(ewf_params *p);
+
+/* Validates sizes and allocates device memory (replaces OK4:428-459 zeros/cudaMalloc). */
+int ewf_create(const ewf_params *p, ewf_handle **out);
+void ewf_destroy(ewf_handle *h);
+int ewf_get_params(const ewf_handle *h, ewf_params *out);
+
+/* Reads pa1/pa2/pa3/MTS/Src and the model files of p->model from p->workdir exactly as
+ * OK4:401-454 (iso) / ANISO:402-487 (ortho), checks their sizes, sets the legacy source cell
+ * (OK4:450-452 / ANISO:483-485, overridable with ewf_set_moment_tensor afterwards) and the 4
+ * legacy receivers (OK4:383-386 / ANISO:263-266). */
+int ewf_load_legacy_inputs(ewf_handle *h);
+
+/* Copies a host array (dtype_bytes 4 = float32, 8 = float64) into a field (replaces
+ * load3 + cudaMemcpy, OK4:195-198).  n must equal the field's element count. */
+int ewf_set_field(ewf_handle *h, int32_t field, const void *host, size_t n, int32_t dtype_bytes);
+/* Snapshot of a field back to the host in the reference layout (replaces gather, OK4:75). */
+int ewf_get_field(ewf_handle *h, int32_t field, void *host, size_t n, int32_t dtype_bytes);
+/* Element count of a field for this grid (0 for an unknown id). */
+size_t ewf_field_size(const ewf_handle *h, int32_t field);
+
+/* Source time function Src[it] (Src.dat, OK4:454); n >= steps that will be run. */
+int ewf_set_stf(ewf_handle *h, const double *stf, size_t n);
+/* Moment tensor (xx,yy,zz,xy,xz,yz) injected at the reference's stencil around cell
+ * (xs,ys,zs): stencil 0 = OK4 offsets (OK4:336-342), 1 = ANISO offsets (ANISO:233-247). */
+int ewf_set_moment_tensor(ewf_handle *h, const double mt[6], int32_t xs, int32_t ys, int32_t zs, int32_t stencil);
+/* General point sources: n entries of (field id 3..8, i, j, k) and coefficients. */
+int ewf_set_sources(ewf_handle *h, int32_t n, const int32_t *comp_ijk, const double *coef);
+/* Receivers: n entries of (i, j, k, field id 0..8), sampled after every velocity update. */
+int ewf_set_receivers(ewf_handle *h, int32_t n, const int32_t *ijk_comp);
+
+/* Number of receivers currently set. */
+int ewf_receiver_count(const ewf_handle *h, int32_t *n);
+
+/* Zeroes the 9 state fields, compensation, traces and the step counter. */
+int ewf_reset(ewf_handle *h);
+/* Advances nsteps time steps (OK4:485-505 / ANISO:519-555); resumable; synchronous. */
+int ewf_run(ewf_handle *h, int32_t nsteps);
+/* Steps completed so far. */
+int ewf_get_step(const ewf_handle *h, int32_t *it);
+/* Receiver traces, FP64, out[r*nt + it] for r < n_rec, it < nt. */
+int ewf_get_seismograms(ewf_handle *h, double *out, size_t n);
+/* Device time of the last ewf_run in milliseconds (CUDA events on the handle's stream). */
+int ewf_last_run_ms(const ewf_handle *h, double *ms);
+
+/* Diagnostics: advances nsteps time steps launching each kernel between CUDA events on the
+ * handle's stream (no graph) and returns the average device time per launch in ms of
+ * out_ms[0] stress, [1] injection, [2] velocity, [3] receiver gather. */
+int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4]);
+/* Number of kernel launches one time step issues. */
+int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
+
+/* Writes 0_infos.inf and 0_0_{Src,Rec,Rec_x,Rec_y,Rec_y2,Vx,Vy,Vz}.res into workdir
+ * (OK4:521-532).  Rec* are the first four receivers. */
+int ewf_write_legacy_outputs(ewf_handle *h);
+/* Writes "<isave>_0_<name>.res" snapshots of Vx, Vy, Vz (the nsave stub of the 16 km scenario). */
+int ewf_write_snapshot(ewf_handle *h, int32_t isave);
+
+/* Checkpoint / resume: state fields, compensation, traces and step counter. */
+int ewf_checkpoint(ewf_handle *h, const char *path);
+int ewf_restore(ewf_handle *h, const char *path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EWFD_H */

@@ -1,0 +1,276 @@
+"""Replays the reference's time loop with the reference's own kernels (TEST INFRASTRUCTURE ONLY).
+
+The kernels come from oracle/_ref/*.cubin, compiled unmodified from the reference sources by
+oracle/build.py; oracle/refkernels.c loads a cubin and launches by name.  This module owns the
+host side the reference's main() would have (FastWaveED_GPU3D_v1.cu:390-559,
+FastWaveED_GPU3D_v1_9kmst_ANISO.cu:391-608): allocation, the launch geometry
+(block (32,2,8), grid covering 64*NB cells per axis, :26-31, 88-89), and the loop order
+  isotropic:     compute_StressPrf, BC1, update_Qxft                    (OK4:485-505)
+  orthorhombic:  compute_StressOrtho, BC1, source, update_VelocityFromStress (ANISO:519-555)
+with our receivers gathered from V after each step (a read-only gather; the reference's own
+hard-coded `record` cells are left as they are).
+
+Allocation differs from the reference in one way: every array carries a zeroed guard of one
+plane on both sides.  The isotropic stress kernel reads Vx/Vy/Vz at i-1, j-1 and k-1 with no
+guard (FastWaveED_GPU3D_v1.cu:323-329); at the grid's low edges those reads fall up to one plane
+before the array (e.g. Vy[ix-1 + ...] = Vy[-1] at the origin).  In the reference run they read
+whatever memory precedes the allocation; here they read the guard, so no access leaves an
+allocation.  The values only reach shear-stress cells the velocity update never reads back.
+
+Requires torch with CUDA (device memory) and the built librefkernels.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from elanfmt_gb300 import fields as F
+from elanfmt_gb300.inputs import separable_weights
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFK = os.path.join(HERE, "librefkernels.so")
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        from . import build as _build
+
+        _build.build_refkernels()
+        L = C.CDLL(REFK)
+        L.refk_error.restype = C.c_char_p
+        L.refk_init.argtypes = [C.c_int]
+        L.refk_load.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+        L.refk_unload.argtypes = [C.c_void_p]
+        L.refk_function.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]
+        L.refk_launch.argtypes = [C.c_void_p] + [C.c_uint] * 6 + [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ck(st: int, what: str) -> None:
+    if st != 0:
+        raise RuntimeError(f"{what}: {lib().refk_error().decode(errors='replace')}")
+
+
+def cubin(model: int, variant: str) -> str:
+    return os.path.join(HERE, "_ref", f"{'ok4' if model == F.MODEL_ISO else 'aniso'}_{variant}.cubin")
+
+
+def available(model: int = F.MODEL_ISO, variant: str = "exact") -> bool:
+    return os.path.exists(cubin(model, variant))
+
+
+class _Args:
+    """Kernel argument vector: ('p', ptr) | ('f', float32) | ('i', int32)."""
+
+    def __init__(self, spec):
+        self.objs = []
+        for kind, v in spec:
+            if kind == "p":
+                self.objs.append(C.c_void_p(int(v)))
+            elif kind == "f":
+                self.objs.append(C.c_float(float(v)))
+            else:
+                self.objs.append(C.c_int32(int(v)))
+        self.argv = (C.c_void_p * len(self.objs))(*[C.cast(C.pointer(o), C.c_void_p) for o in self.objs])
+
+    def set_int(self, pos: int, v: int) -> None:
+        self.objs[pos].value = int(v)
+
+
+class RefRunner:
+    """Reference kernels on one Model (iso: OK4 stencil + before-BC1 order; ortho: the ANISO
+    stencil with ANISO's built-in tensor, after-BC1 order, 3-D weights)."""
+
+    def __init__(self, m, variant: str = "exact", device: int = 0):
+        import torch
+
+        self.torch = torch
+        self.m = m
+        self.dev = torch.device("cuda", device)
+        torch.cuda.init()
+        torch.zeros(1, device=self.dev)
+        _ck(lib().refk_init(device), "refk_init")
+        mod = C.c_void_p()
+        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant)), C.byref(mod)), "refk_load")
+        self.mod = mod
+        nx, ny, nz = m.nx, m.ny, m.nz
+        self.pad = (nx + 2) * (ny + 2) + 64
+        self._bufs = []
+        self.nbx = math.ceil(nx / 64)
+        self.nby = math.ceil(ny / 64)
+        self.nbz = math.ceil(nz / 64)
+        if nx > ny and 64 * self.nby > ny:
+            raise ValueError("reference BC1 with nx > ny writes past row ny (a race): use nx <= ny or ny % 64 == 0")
+        self.grid = (2 * self.nbx, 32 * self.nby, 8 * self.nbz)
+        self.block = (32, 2, 8)
+        self.f = [self._alloc(F.shape(q, nx, ny, nz)) for q in F.STATE]
+        self.dummy = self._alloc((1024,))
+        self.rec_dummy = [self._alloc((m.nt,)) for _ in range(4)]
+        self.src = self._upload(np.asarray(m.stf[: m.nt], np.float32)) if m.stf is not None else self._alloc((m.nt,))
+        nrec = 0 if m.receivers is None else len(m.receivers)
+        self.traces = np.zeros((nrec, m.nt), np.float64)
+        if nrec:
+            offs, comps = [], []
+            for i, j, k, c in m.receivers:
+                ez, ey, ex = F.shape(int(c), nx, ny, nz)
+                offs.append(int(i) + ex * (int(j) + ey * int(k)))
+                comps.append(int(c))
+            self.rec_off = torch.tensor(offs, device=self.dev)
+            self.rec_comp = comps
+        self.it = 0
+        self._setup_kernels()
+
+    # -- memory ---------------------------------------------------------------------------------
+    def _alloc(self, shape):
+        n = int(np.prod(shape))
+        t = self.torch.zeros(n + 2 * self.pad, dtype=self.torch.float32, device=self.dev)
+        self._bufs.append(t)
+        view = t[self.pad: self.pad + n]
+        return view
+
+    def _upload(self, arr):
+        a = np.ascontiguousarray(arr, np.float32).ravel()
+        v = self._alloc(a.shape)
+        v.copy_(self.torch.from_numpy(a))
+        return v
+
+    @staticmethod
+    def _p(t) -> int:
+        return t.data_ptr()
+
+    def _fn(self, prefix: str):
+        f = C.c_void_p()
+        _ck(lib().refk_function(self.mod, prefix.encode(), C.byref(f)), prefix)
+        return f
+
+    # -- kernels --------------------------------------------------------------------------------
+    def _check_sources(self, stencil: int):
+        m = self.m
+        if m.sources is None or len(m.sources) == 0:
+            raise ValueError("the reference kernels always inject: the model needs a source")
+        ent = np.asarray(m.sources)
+        xs, ys, zs = int(ent[0, 1]) - 1, int(ent[0, 2]) - 1, int(ent[0, 3]) - 1
+        want, coef = F.mt_entries(np.zeros(6), xs, ys, zs, stencil)
+        if not np.array_equal(want, ent):
+            raise ValueError("sources must be the reference's moment-tensor stencil")
+        return xs, ys, zs
+
+    def _setup_kernels(self):
+        m = self.m
+        P = self._p
+        f = self.f
+        nx, ny, nz = m.nx, m.ny, m.nz
+        d = self.dummy
+        if m.model == F.MODEL_ISO:
+            if m.src_order != F.SRC_BEFORE_BC1 or m.damping != F.DAMP_PML1D:
+                raise ValueError("isotropic reference = before-BC1 injection and 1-D PML")
+            xs, ys, zs = self._check_sources(0)
+            mt = {int(c): float(v) for (c, *_), v in zip(m.sources, m.source_coef)}
+            c11 = self._upload(m.materials[F.M_C11])
+            c12 = self._upload(m.materials[F.M_C12])
+            wx, wy, wz = (self._upload(m.damping_arrays[k]) for k in (F.D_WX, F.D_WY, F.D_WZ))
+            R = self.rec_dummy
+            self.k_stress = self._fn("_Z17compute_StressPrf")
+            self.a_stress = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 3
+                + [("p", P(c11)), ("p", P(c12)), ("p", P(wx)), ("p", P(wy)), ("p", P(wz))]
+                + [("p", P(r)) for r in R] + [("p", P(self.src))]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 8 + [("f", m.c66)]
+                + [("f", 0.0)] * 4
+                + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)]
+                + [("f", mt[F.F_SXX]), ("f", mt[F.F_SYY]), ("f", mt[F.F_SZZ]), ("f", mt[F.F_SXY]),
+                   ("f", mt[F.F_SXZ]), ("f", mt[F.F_SYZ])])
+            self.it_pos_stress = 23 + 17 + 3
+            self.k_vel = self._fn("_Z11update_Qxft")
+            self.a_vel = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 7
+                + [("p", P(wx)), ("p", P(wy)), ("p", P(wz))] + [("p", P(r)) for r in R]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt), ("f", 0.0), ("f", 0.0), ("f", 0.0),
+                   ("f", m.bx), ("f", m.by), ("f", m.bz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5), ("i", 0)])
+            self.it_pos_vel = 24 + 16 + 3 + 1
+            self.k_src = None
+        else:
+            if m.src_order != F.SRC_AFTER_BC1:
+                raise ValueError("orthorhombic reference = after-BC1 injection")
+            xs, ys, zs = self._check_sources(1)
+            coef = tuple(float(np.float32(v)) for v in self._mt_tuple())
+            if coef != F.ANISO_LEGACY_MT:
+                raise ValueError("the orthorhombic reference hard-codes its tensor: use fields.ANISO_LEGACY_MT")
+            mats = [self._upload(m.materials[k]) for k in F.ORTHO_MATERIALS]
+            if F.D_W3D in m.damping_arrays:
+                W = self._upload(m.damping_arrays[F.D_W3D])
+            else:
+                W = self._upload(separable_weights(m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY],
+                                                   m.damping_arrays[F.D_WZ]))
+            C11, C22, C33, C12, C13, C23, C66, C55, C44, BX, BY, BZ = mats
+            self.k_stress = self._fn("_Z19compute_StressOrtho")
+            self.a_stress = _Args(
+                [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)]
+                + [("p", P(x)) for x in (C11, C22, C33, C12, C13, C23, C66, C55, C44, W)]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt), ("i", nx), ("i", ny), ("i", nz)])
+            self.it_pos_stress = None
+            self.k_src = self._fn("_Z6source")
+            self.a_src = _Args(
+                [("p", P(d))] * 4 + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1)] + [("p", P(d))] * 2
+                + [("p", P(self.src))] + [("f", m.dx), ("f", m.dy), ("f", m.dz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)]
+                + [("f", m.dt)])
+            self.it_pos_src = 15 + 9 + 3
+            self.k_vel = self._fn("_Z25update_VelocityFromStress")
+            self.a_vel = _Args(
+                [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(x)) for x in (BX, BY, BZ, W)]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt), ("i", nx), ("i", ny), ("i", nz)])
+            self.it_pos_vel = None
+        self.k_bc1 = self._fn("_Z3BC1")
+        self.a_bc1 = _Args(
+            [("p", P(d))] * 4 + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 2
+            + [("p", P(self.rec_dummy[0]))] + [("f", m.dx), ("f", m.dy), ("f", m.dz)] + [("f", 0.0)] * 6
+            + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", 0), ("i", 0), ("i", 0), ("i", 2)] + [("f", m.dt)])
+        self.it_pos_bc1 = 16 + 9 + 3
+
+    def _mt_tuple(self):
+        mt = {int(c): float(v) for (c, *_), v in zip(self.m.sources, self.m.source_coef)}
+        return (mt[F.F_SXX], mt[F.F_SYY], mt[F.F_SZZ], mt[F.F_SXY], mt[F.F_SXZ], mt[F.F_SYZ])
+
+    def _launch(self, fn, args):
+        _ck(lib().refk_launch(fn, *self.grid, *self.block, args.argv), "launch")
+
+    def run(self, nsteps: int) -> None:
+        torch = self.torch
+        for _ in range(nsteps):
+            it = self.it
+            if self.it_pos_stress is not None:
+                self.a_stress.set_int(self.it_pos_stress, it)
+            self._launch(self.k_stress, self.a_stress)
+            self.a_bc1.set_int(self.it_pos_bc1, it)
+            self._launch(self.k_bc1, self.a_bc1)
+            if self.k_src is not None:
+                self.a_src.set_int(self.it_pos_src, it)
+                self._launch(self.k_src, self.a_src)
+            if self.it_pos_vel is not None:
+                self.a_vel.set_int(self.it_pos_vel, it)
+            self._launch(self.k_vel, self.a_vel)
+            _ck(lib().refk_sync(), "sync")
+            if len(self.traces):
+                vals = [self.f[c][int(o)] for c, o in zip(self.rec_comp, self.rec_off.tolist())]
+                self.traces[:, it] = torch.stack(vals).double().cpu().numpy()
+            self.it += 1
+        torch.cuda.synchronize()
+
+    def fields(self) -> list[np.ndarray]:
+        m = self.m
+        return [self.f[q].cpu().numpy().reshape(F.shape(q, m.nx, m.ny, m.nz)) for q in F.STATE]
+
+    def close(self):
+        if self.mod:
+            lib().refk_unload(self.mod)
+            self.mod = None
+        self._bufs.clear()

@@ -1,0 +1,173 @@
+"""Product kernels (libewfd.so on the GPU) against the CPU oracle.
+
+The product's device code is built without FMA contraction and keeps the reference's operand
+order, as does the oracle (gcc -ffp-contract=off): the FP32, FP32-compensated and FP64 runs must
+agree BIT FOR BIT on every state field and every receiver sample.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from elanfmt_gb300 import fields as F
+from elanfmt_gb300 import inputs as I
+from elanfmt_gb300 import legacy as L
+from elanfmt_gb300.solver import EwfError, Solver
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def product(m, nsteps, prec=F.PREC_F32, chunks=None, **kw):
+    dt = np.float64 if prec == F.PREC_F64 else np.float32
+    with Solver.from_model(m, precision=prec, **kw) as s:
+        for n in (chunks or [nsteps]):
+            s.run(n)
+        return [s.field(q, dt) for q in F.STATE], s.seismograms()
+
+
+def assert_bitwise(prod, ref, what=""):
+    fields, traces = prod
+    for q in F.STATE:
+        a, b = fields[q], ref.f[q]
+        if not np.array_equal(a, b):
+            d = np.argwhere(a != b)
+            raise AssertionError(f"{what} field {F.STATE_NAMES[q]}: {len(d)} cells differ, first {d[:3].tolist()} "
+                                 f"{a[tuple(d[0])]} vs {b[tuple(d[0])]}")
+    np.testing.assert_array_equal(traces, ref.traces, err_msg=f"{what} traces")
+    assert np.abs(traces).max() > 0, "degenerate case: receivers saw nothing"
+
+
+CASES = [
+    ("iso", F.MODEL_ISO, None, 37, 41, 23),
+    ("iso-ragged", F.MODEL_ISO, None, 33, 9, 31),
+    ("ortho-w3d", F.MODEL_ORTHO, F.DAMP_W3D, 35, 40, 21),
+    ("ortho-sep", F.MODEL_ORTHO, F.DAMP_SEPARABLE, 29, 30, 27),
+]
+
+
+@pytest.mark.parametrize("name,model,damping,nx,ny,nz", CASES, ids=[c[0] for c in CASES])
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
+def test_bitwise_vs_oracle(cuda_device, name, model, damping, nx, ny, nz, prec):
+    m = I.random_small(model, nx, ny, nz, nt=48, seed=nx * 7 + nz, damping=damping)
+    ref = O.run(m, 48, prec)
+    assert_bitwise(product(m, 48, prec), ref, name)
+
+
+@pytest.mark.parametrize("order", [F.SRC_BEFORE_BC1, F.SRC_AFTER_BC1])
+@pytest.mark.parametrize("stencil", [0, 1])
+@pytest.mark.parametrize("zs", [0, 1, 5])
+def test_source_next_to_free_surface(cuda_device, order, stencil, zs):
+    """Injection on planes 1-2 interacts with BC1 (before-BC1 order drops / propagates it)."""
+    for model in (F.MODEL_ISO, F.MODEL_ORTHO):
+        m = I.random_small(model, 24, 26, 18, nt=30, seed=3 + zs, src_order=order, stencil=stencil)
+        m.set_moment_tensor(np.array([1.0, -0.5, 0.25, 0.7, -0.9, 1.3]), 10, 11, zs, stencil)
+        ref = O.run(m, 30)
+        assert_bitwise(product(m, 30), ref, f"model {model} order {order} stencil {stencil} zs {zs}")
+
+
+@pytest.mark.parametrize("kchunk,graph_steps", [(4, -1), (7, 5), (16, 0), (64, 64), (5, 3)])
+def test_tiling_and_graph_do_not_change_results(cuda_device, kchunk, graph_steps):
+    m = I.random_small(F.MODEL_ORTHO, 40, 33, 29, nt=40, seed=11, damping=F.DAMP_SEPARABLE)
+    ref = O.run(m, 40)
+    assert_bitwise(product(m, 40, kchunk=kchunk, graph_steps=graph_steps, chunks=[13, 20, 7]), ref)
+
+
+def test_workload_shapes_small(cuda_device):
+    """The two benchmark workloads at reduced size, FP32, bit-exact."""
+    m = I.iso_homogeneous(n=48, nt=120)
+    assert_bitwise(product(m, 120), O.run(m, 120), "iso48")
+    m = I.ortho_layered(nx=48, ny=48, nz=40, nt=60, src=(24, 24, 4), rec_coords=[4, 20, 40])
+    assert_bitwise(product(m, 60), O.run(m, 60), "ortho48")
+
+
+def test_reset_restart_and_checkpoint(cuda_device, tmp_path):
+    m = I.random_small(F.MODEL_ISO, 30, 30, 20, nt=50, seed=5)
+    ref = O.run(m, 50)
+    with Solver.from_model(m) as s:
+        s.run(20)
+        ck = str(tmp_path / "run.ckpt")
+        s.checkpoint(ck)
+        s.run(30)
+        full = ([s.field(q) for q in F.STATE], s.seismograms())
+        assert_bitwise(full, ref, "uninterrupted")
+        s.reset()
+        assert s.step() == 0
+        assert np.abs(s.field(F.F_VX)).max() == 0
+        s.restore(ck)
+        assert s.step() == 20
+        s.run(30)
+        assert_bitwise(([s.field(q) for q in F.STATE], s.seismograms()), ref, "resumed")
+    # a fresh handle restored from the file resumes bit-exactly too
+    with Solver.from_model(m) as s2:
+        s2.restore(ck)
+        s2.run(30)
+        assert_bitwise(([s2.field(q) for q in F.STATE], s2.seismograms()), ref, "resumed in new handle")
+
+
+def test_errors_are_status_codes(cuda_device):
+    m = I.random_small(F.MODEL_ISO, 20, 20, 16, nt=10, seed=1)
+    with Solver.from_model(m) as s:
+        with pytest.raises(EwfError) as e:
+            s.run(11)  # past nt
+        assert e.value.status == -1
+        with pytest.raises(EwfError):
+            s.set_field(F.M_C11, np.zeros((3, 3, 3), np.float32))
+        with pytest.raises(EwfError):
+            s.set_receivers(np.array([[20, 0, 0, 0]]))  # Vx has nx+1 = 21 cells in x: ok
+            s.set_receivers(np.array([[21, 0, 0, 0]]))
+        with pytest.raises(EwfError):
+            s.set_sources(np.array([[0, 1, 1, 1]]), np.array([1.0]))  # not a stress field
+    m.materials[F.M_C11] = m.materials[F.M_C11].copy()
+    m.materials[F.M_C11][5, 5, 5] = np.nan
+    with Solver.from_model(m) as s:
+        with pytest.raises(EwfError) as e:
+            s.run(10)
+        assert e.value.status == -7  # non-finite traces detected on the host
+    # inputs missing
+    with Solver.from_model(I.random_small(F.MODEL_ISO, 20, 20, 16, nt=10, seed=1)) as s0:
+        params = s0.params
+    with Solver(params) as s:
+        with pytest.raises(EwfError) as e:
+            s.run(1)
+        assert e.value.status == -5
+
+
+def test_legacy_file_contract_through_ewfd(cuda_device, tmp_path):
+    """MATLAB-style inputs in, ewfd run, 0_infos.inf + 0_0_*.res out; compared with the oracle."""
+    m = I.random_small(F.MODEL_ISO, 40, 44, 24, nt=40, seed=9)
+    xs, ys, zs = 12, 13, 9
+    m.set_moment_tensor(np.array([0.5, -1.0, 0.3, 0.2, 1.0, 0.8]), xs, ys, zs, 0)
+    m.receivers = np.array([[30, 20, 1, F.F_VZ], [30, 20, 1, F.F_VX], [30, 23, 1, F.F_VY], [30, 22, 1, F.F_VY],
+                            [5, 6, 7, F.F_VZ]], np.int32)
+    L.write_inputs(m, str(tmp_path))
+    with open(tmp_path / "rec.txt", "w") as fh:
+        for r in m.receivers:
+            fh.write(" ".join(str(int(v)) for v in r) + "\n")
+    exe = os.path.join(ROOT, "elanfmt_gb300", "ewfd")
+    r = subprocess.run([exe, "--nx", "40", "--ny", "44", "--nz", "24", "--workdir", str(tmp_path), "--src",
+                        f"{xs},{ys},{zs}", "--receivers", str(tmp_path / "rec.txt"), "--quiet"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = L.read_outputs(str(tmp_path), m.nt)
+    assert out["PRECIS"] == 4 and (out["nx"], out["ny"], out["nz"]) == (40, 44, 24)
+    ref = O.run(m, 40)
+    np.testing.assert_array_equal(out["Vx"], ref.f[F.F_VX])
+    np.testing.assert_array_equal(out["Vy"], ref.f[F.F_VY])
+    np.testing.assert_array_equal(out["Vz"], ref.f[F.F_VZ])
+    for q, name in enumerate(("Rec", "Rec_x", "Rec_y", "Rec_y2")):
+        np.testing.assert_array_equal(out[name], ref.traces[q].astype(np.float32))
+    np.testing.assert_array_equal(out["Rec_all"], ref.traces.astype(np.float32))
+    np.testing.assert_array_equal(out["Src"], m.stf[: m.nt].astype(np.float32))
+    # the same through the Python mirror of the executable
+    s = Solver.legacy(str(tmp_path), 40, 44, 24)
+    try:
+        s.set_moment_tensor(np.fromfile(tmp_path / "MTS.dat", np.float32).astype(np.float64), xs, ys, zs, 0)
+        s.set_receivers(m.receivers)
+        s.run(40)
+        np.testing.assert_array_equal(s.seismograms(), ref.traces)
+    finally:
+        s.close()
