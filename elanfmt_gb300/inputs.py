@@ -61,14 +61,14 @@ def sponge_3d_legacy(nx: int, ny: int, nz: int, thick: int = 120, margin_y: int 
     return np.exp(-rr).astype(np.float32)
 
 
-def separable_weights(px: np.ndarray, py: np.ndarray, pz: np.ndarray) -> np.ndarray:
-    """The 3-D weight field W[k,j,i] = (px[i]*py[j])*pz[k] in float32 arithmetic -- bit-identical
-    to what the separable-damping kernels form on the fly."""
-    px = np.asarray(px, np.float32)
-    py = np.asarray(py, np.float32)
-    pz = np.asarray(pz, np.float32)
+def separable_weights(px: np.ndarray, py: np.ndarray, pz: np.ndarray, dtype=np.float32) -> np.ndarray:
+    """The 3-D weight field W[k,j,i] = (px[i]*py[j])*pz[k] in `dtype` arithmetic -- bit-identical
+    to what the separable-damping kernels of that precision form on the fly."""
+    px = np.asarray(px, dtype)
+    py = np.asarray(py, dtype)
+    pz = np.asarray(pz, dtype)
     pxy = py[:, None] * px[None, :]
-    return (pxy[None, :, :] * pz[:, None, None]).astype(np.float32)
+    return (pxy[None, :, :] * pz[:, None, None]).astype(dtype)
 
 
 def pml_factors(n: int, lpml: int, dt: float, R: float = 1e-8, sides: str = "both") -> np.ndarray:

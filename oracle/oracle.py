@@ -98,8 +98,8 @@ class Runner:
             if F.D_W3D in m.damping_arrays:
                 self.W = cv(m.damping_arrays[F.D_W3D])
             else:
-                self.W = cv(separable_weights(m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY],
-                                              m.damping_arrays[F.D_WZ]))
+                self.W = separable_weights(m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY],
+                                           m.damping_arrays[F.D_WZ], dtype)
         self.src = np.ascontiguousarray(m.sources if m.sources is not None else np.zeros((0, 4)), np.int32)
         self.coef = np.ascontiguousarray(m.source_coef if m.source_coef is not None else np.zeros(0), np.float64)
         self.stf = np.ascontiguousarray(m.stf if m.stf is not None else np.zeros(m.nt), np.float64)

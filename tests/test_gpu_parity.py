@@ -122,7 +122,7 @@ def test_errors_are_status_codes(cuda_device):
         with pytest.raises(EwfError):
             s.set_sources(np.array([[0, 1, 1, 1]]), np.array([1.0]))  # not a stress field
     m.materials[F.M_C11] = m.materials[F.M_C11].copy()
-    m.materials[F.M_C11][5, 5, 5] = np.nan
+    m.materials[F.M_C11][1, 10, 10] = np.nan  # next to the receiver at (10, 10, 1)
     with Solver.from_model(m) as s:
         with pytest.raises(EwfError) as e:
             s.run(10)
