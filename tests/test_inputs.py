@@ -117,9 +117,14 @@ def test_lune():
 
 
 def test_rotate_mt_matches_reference_values():
-    # runmerotation.m rotates its tensor by 139 degrees to give the orthorhombic solver's
-    # hard-coded coefficients (FastWaveED_GPU3D_v1_9kmst_ANISO.cu:233-247); check the rotation
-    # preserves invariants and is an involution with its inverse
+    # known answer from the reference: runmerotation.m:200-207 rotates this tensor by 139 degrees
+    # and its comment at :146-148 lists the result, which is also the tensor the orthorhombic
+    # solver hard-codes (FastWaveED_GPU3D_v1_9kmst_ANISO.cu:233-247)
+    src = np.array([0.4895, -0.1740, 0.2439, 0.8403, 0.3594, 0.0005])  # xx yy zz xy xz yz
+    want = np.array([-0.6282, 0.9437, 0.2439, 0.4455, -0.2709, -0.2362])
+    np.testing.assert_allclose(I.rotate_mt(src, 139.0), want, atol=1.5e-4)
+    np.testing.assert_allclose(np.array(F.ANISO_LEGACY_MT), want, atol=1e-7)
+    # and the rotation preserves invariants and inverts
     mt = np.array([0.3, -0.5, 0.2, 0.1, -0.4, 0.25])
     r = I.rotate_mt(I.rotate_mt(mt, 139.0), -139.0)
     assert np.allclose(r, mt)
