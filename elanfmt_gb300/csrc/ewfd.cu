@@ -11,6 +11,7 @@
 
 #include <cmath>
 #include <cstdarg>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -871,4 +872,67 @@ extern "C" int ewf_restore(ewf_handle *h, const char *path)
         h->it = it;
     }
     return st;
+}
+
+// ------------------------------------------------------------------------------------------
+// Layout conversion without device allocation (ewf_pack_field_noalloc).  The staging scratch
+// that ewf_set_field takes from its handle is, here, a fixed array compiled into the library;
+// host code only ever passes the array's device address, looked up once per device.
+// ------------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_pack_scratch[EWF_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_pack_scratch_mu;
+void *g_pack_scratch_addr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of g_pack_scratch on the current device (looked up on first use).
+static int pack_scratch_address(void **out)
+{
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return ewf_fail(EWF_ERR_UNSUPPORTED, "device ordinal %d >= %d", dev, kMaxDevices);
+    std::lock_guard<std::mutex> lock(g_pack_scratch_mu);
+    if (!g_pack_scratch_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_pack_scratch);
+        if (e != cudaSuccess || !p)
+            return ewf_fail(EWF_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
+        g_pack_scratch_addr[dev] = p;
+    }
+    *out = g_pack_scratch_addr[dev];
+    return EWF_OK;
+}
+
+extern "C" int ewf_pack_field_noalloc(void *dst, int32_t dst_dtype_bytes, int32_t sx, int64_t sy, const void *host,
+                                      int32_t host_dtype_bytes, int32_t ex, int32_t ey, int32_t ez, void *stream)
+{
+    if (!dst || !host) return ewf_fail(EWF_ERR_ARG, "NULL pointer");
+    if ((dst_dtype_bytes != 4 && dst_dtype_bytes != 8) || (host_dtype_bytes != 4 && host_dtype_bytes != 8))
+        return ewf_fail(EWF_ERR_ARG, "dtype bytes must be 4 or 8");
+    if (ex < 1 || ey < 1 || ez < 1) return ewf_fail(EWF_ERR_ARG, "extent %dx%dx%d", ex, ey, ez);
+    if (sx < ex || sy < (int64_t)sx * ey)
+        return ewf_fail(EWF_ERR_ARG, "pitches sx=%d sy=%lld do not hold %dx%d rows", sx, (long long)sy, ex, ey);
+    const size_t n = (size_t)ex * ey * ez;
+    const size_t bytes = n * (size_t)host_dtype_bytes;
+    if (bytes > EWF_NOALLOC_SCRATCH_BYTES)
+        return ewf_fail(EWF_ERR_ARG, "array of %zu bytes exceeds the %u-byte no-allocation scratch", bytes,
+                        (unsigned)EWF_NOALLOC_SCRATCH_BYTES);
+    void *scratch = nullptr;
+    const int st = pack_scratch_address(&scratch);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(scratch, host, bytes, cudaMemcpyHostToDevice, s));
+    const unsigned nb = pack_blocks(n);
+    if (dst_dtype_bytes == 4) {
+        if (host_dtype_bytes == 4) k_pack<float, float><<<nb, 256, 0, s>>>((float *)dst, (const float *)scratch, ex, ey, ez, sx, sy);
+        else k_pack<float, double><<<nb, 256, 0, s>>>((float *)dst, (const double *)scratch, ex, ey, ez, sx, sy);
+    } else {
+        if (host_dtype_bytes == 4) k_pack<double, float><<<nb, 256, 0, s>>>((double *)dst, (const float *)scratch, ex, ey, ez, sx, sy);
+        else k_pack<double, double><<<nb, 256, 0, s>>>((double *)dst, (const double *)scratch, ex, ey, ez, sx, sy);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return EWF_OK;
 }

@@ -66,6 +66,8 @@ SIGNATURES = {
     "ewf_launches_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_write_legacy_outputs": (C.c_int, [C.c_void_p]),
     "ewf_write_snapshot": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_pack_field_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int32,
+                                         C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ewf_restore": (C.c_int, [C.c_void_p, C.c_char_p]),
 }

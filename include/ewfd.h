@@ -171,6 +171,28 @@ int ewf_write_legacy_outputs(ewf_handle *h);
 /* Writes "<isave>_0_<name>.res" snapshots of Vx, Vy, Vz (the nsave stub of the 16 km scenario). */
 int ewf_write_snapshot(ewf_handle *h, int32_t isave);
 
+/* Layout conversion that allocates nothing (no counterpart in the reference).
+ *
+ * Some callers cannot call cudaMalloc: a host application whose device memory is already
+ * handed out by another framework's pool (a MATLAB gpuArray, a caching allocator that reserved
+ * the GPU up front) or that runs under a fixed device-memory budget.  They own the device array
+ * and want the solver's layout in it.  This copies a host array in the reference layout
+ * (ex x ey x ez, x fastest, float32 or float64) into the caller's device array `dst` in the box
+ * layout of the kernels -- element (i,j,k) at dst[i + j*sx + k*sy], converted to
+ * dst_dtype_bytes -- the same conversion ewf_set_field does.  Its only scratch is a fixed
+ * EWF_NOALLOC_SCRATCH_BYTES array compiled into the library (every GPU that loads the library
+ * holds it until exit); arrays larger than that are rejected with EWF_ERR_ARG.  It calls no
+ * cudaMalloc/cudaFree.  `stream` is a cudaStream_t (NULL = the default stream); the call
+ * returns once the copy is complete.
+ *   - The first call on a device looks up the scratch's device address on that device (with
+ *     it current); make that first call before any stream capture.
+ *   - All calls share the one scratch array: calls that overlap on the GPU (from several host
+ *     threads or streams) race.  Only dst's cells inside the extent are written.
+ */
+#define EWF_NOALLOC_SCRATCH_BYTES (16u << 20)
+int ewf_pack_field_noalloc(void *dst, int32_t dst_dtype_bytes, int32_t sx, int64_t sy, const void *host,
+                           int32_t host_dtype_bytes, int32_t ex, int32_t ey, int32_t ez, void *stream);
+
 /* Checkpoint / resume: state fields, compensation, traces and step counter. */
 int ewf_checkpoint(ewf_handle *h, const char *path);
 int ewf_restore(ewf_handle *h, const char *path);
