@@ -310,7 +310,7 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     h->sy = (long long)h->sx * py;
     h->box_elems = (size_t)h->sy * pz;
     h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
-    h->kchunk = p->kchunk > 0 ? p->kchunk : (nz >= 256 ? 32 : 16);
+    h->kchunk = p->kchunk > 0 ? p->kchunk : 16;
     h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
 
 #define CKH(call)                                                                                    \

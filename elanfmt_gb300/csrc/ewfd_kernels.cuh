@@ -58,7 +58,49 @@ __device__ __forceinline__ T ld(const T *p) { return __ldg(p); }
 
 // ---------------------------------------------------------------------------------------------
 // Stress update.  Isotropic: OK4:285-331.  Orthorhombic: ANISO:287-356.  BC1: OK4:271-283.
+//
+// Each thread marches its (i,j) column over the CTA's planes.  All loads of a plane sit in one
+// branch-free block (the box layout makes every neighbour read in-bounds) and the next plane's
+// loads are issued before the current plane is computed, so ~25 independent loads per thread
+// are always in flight; conditional updates become predicated stores.
 // ---------------------------------------------------------------------------------------------
+template <typename T, int MODEL>
+struct StressIn {
+    T vx, vx_ip, vx_jm;        // Vx(i,j,k), Vx(i+1), Vx(j-1)
+    T vy, vy_jp, vy_im;        // Vy(i,j,k), Vy(j+1), Vy(i-1)
+    T vz_p, vz_im, vz_jm;      // Vz(k+1), Vz(i-1,k), Vz(j-1,k)
+    T s[6];                    // sxx syy szz sxy sxz syz at (i,j,k)
+    T c[MODEL == MODEL_ISO ? 2 : 9];
+    T w;                       // iso: wz[k+1]; ortho: W or pz[k]
+};
+
+template <typename T, int MODEL, int DAMP>
+__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, int k, StressIn<T, MODEL> &q)
+{
+    const int sx = a.sx;
+    const long long sy = a.sy;
+    q.vx = ld(a.f[0] + c);
+    q.vx_ip = ld(a.f[0] + c + 1);
+    q.vx_jm = ld(a.f[0] + c - sx);
+    q.vy = ld(a.f[1] + c);
+    q.vy_jp = ld(a.f[1] + c + sx);
+    q.vy_im = ld(a.f[1] + c - 1);
+    q.vz_p = ld(a.f[2] + c + sy);
+    q.vz_im = ld(a.f[2] + c - 1);
+    q.vz_jm = ld(a.f[2] + c - sx);
+#pragma unroll
+    for (int f = 0; f < 6; ++f) q.s[f] = a.f[3 + f][c];
+    if (MODEL == MODEL_ISO) {
+        q.c[0] = ld(a.m[0] + c);
+        q.c[1] = ld(a.m[1] + c);
+        q.w = ld(a.w1[2] + k + 1);
+    } else {
+#pragma unroll
+        for (int f = 0; f < 9; ++f) q.c[f] = ld(a.m[f] + c);
+        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + c) : ld(a.w1[2] + k);
+    }
+}
+
 template <typename T, int MODEL, int DAMP>
 __global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
 {
@@ -69,17 +111,6 @@ __global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
     const int k1 = min(k0 + a.kchunk, a.nz);
     const int sx = a.sx;
     const long long sy = a.sy;
-    const long long c0 = (long long)i + (long long)j * sx + (long long)k0 * sy;
-
-    const T *__restrict__ Vx = a.f[0];
-    const T *__restrict__ Vy = a.f[1];
-    const T *__restrict__ Vz = a.f[2];
-    T *__restrict__ sxx = a.f[3];
-    T *__restrict__ syy = a.f[4];
-    T *__restrict__ szz = a.f[5];
-    T *__restrict__ sxy = a.f[6];
-    T *__restrict__ sxz = a.f[7];
-    T *__restrict__ syz = a.f[8];
     const T dt = a.dt, rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
 
     // damping factors constant along the column
@@ -94,76 +125,69 @@ __global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
     }
     const bool row_bc = (j < a.bc1_rows);
 
-    // z-rotation registers
-    long long c = c0;
-    T vx_m = ld(Vx + c - sy);  // Vx(k-1)
-    T vy_m = ld(Vy + c - sy);  // Vy(k-1)
-    T vz_k = ld(Vz + c);       // Vz(k)
+    long long c = (long long)i + (long long)j * sx + (long long)k0 * sy;
+    T vx_m = ld(a.f[0] + c - sy);  // Vx(k-1)
+    T vy_m = ld(a.f[1] + c - sy);  // Vy(k-1)
+    T vz_k = ld(a.f[2] + c);       // Vz(k)
     T wz_k = T(0);
     if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + k0);
+    StressIn<T, MODEL> nxt;
+    stress_load<T, MODEL, DAMP>(a, c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sy) {
-        const T vx_k = ld(Vx + c);
-        const T vy_k = ld(Vy + c);
-        const T vz_p = ld(Vz + c + sy);
-        const T Vxx = (ld(Vx + c + 1) - vx_k) * rdx;
-        const T Vyy = (ld(Vy + c + sx) - vy_k) * rdy;
-        const T Vzz = (vz_p - vz_k) * rdz;
-        T sxz_new = T(0), syz_new = T(0);
+        const StressIn<T, MODEL> q = nxt;
+        if (k + 1 < k1) stress_load<T, MODEL, DAMP>(a, c + sy, k + 1, nxt);
+        const T Vxx = (q.vx_ip - q.vx) * rdx;
+        const T Vyy = (q.vy_jp - q.vy) * rdy;
+        const T Vzz = (q.vz_p - vz_k) * rdz;
+        T sxx, syy, szz, sxy, sxz, syz;
+        bool w_xy = true, w_xz = true, w_yz = true;
         if (MODEL == MODEL_ISO) {
-            const T wz_p = ld(a.w1[2] + k + 1);
-            const T c11 = ld(a.m[0] + c), c12 = ld(a.m[1] + c);
+            const T c11 = q.c[0], c12 = q.c[1];
             // OK4:307-309
-            sxx[c] = wavx * (sxx[c] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
-            syy[c] = wavy * (syy[c] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
-            const T szz_new = T(0.5) * (wz_p + wz_k) * (szz[c] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
-            szz[c] = (k == 0 && row_bc) ? T(0) : szz_new;
+            sxx = wavx * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
+            syy = wavy * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
+            szz = T(0.5) * (q.w + wz_k) * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
             const T c66dt = a.c66 * dt;
             // OK4:323, 326, 329 (no guards: zero-padded neighbours at the low edges)
-            sxy[c] = wz_k * wyj * wxi * (sxy[c] + c66dt * ((vy_k - ld(Vy + c - 1)) * rdx + (vx_k - ld(Vx + c - sx)) * rdy));
-            sxz_new = wyj * wz_k * wxi * (sxz[c] + c66dt * ((vz_k - ld(Vz + c - 1)) * rdx + (vx_k - vx_m) * rdz));
-            sxz[c] = sxz_new;
-            syz_new = wxi * wyj * wz_k * (syz[c] + c66dt * ((vy_k - vy_m) * rdz + (vz_k - ld(Vz + c - sx)) * rdy));
-            syz[c] = syz_new;
-            wz_k = wz_p;
+            sxy = wz_k * wyj * wxi * (q.s[3] + c66dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
+            sxz = wyj * wz_k * wxi * (q.s[4] + c66dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
+            syz = wxi * wyj * wz_k * (q.s[5] + c66dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
+            wz_k = q.w;
         } else {
-            T W;
-            if (DAMP == DAMP_W3D) W = ld(a.w3 + c);
-            else W = pxy * ld(a.w1[2] + k);
-            const T C11 = ld(a.m[0] + c), C22 = ld(a.m[1] + c), C33 = ld(a.m[2] + c);
-            const T C12 = ld(a.m[3] + c), C13 = ld(a.m[4] + c), C23 = ld(a.m[5] + c);
-            // ANISO:312-325
-            sxx[c] = sxx[c] * W + dt * (C11 * Vxx + C12 * Vyy + C13 * Vzz);
-            syy[c] = syy[c] * W + dt * (C12 * Vxx + C22 * Vyy + C23 * Vzz);
-            const T szz_new = szz[c] * W + dt * (C13 * Vxx + C23 * Vyy + C33 * Vzz);
-            szz[c] = (k == 0 && row_bc) ? T(0) : szz_new;
+            const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
+            // ANISO:312-325 (c[]: C11 C22 C33 C12 C13 C23 C66 C55 C44)
+            sxx = q.s[0] * W + dt * (q.c[0] * Vxx + q.c[3] * Vyy + q.c[4] * Vzz);
+            syy = q.s[1] * W + dt * (q.c[3] * Vxx + q.c[1] * Vyy + q.c[5] * Vzz);
+            szz = q.s[2] * W + dt * (q.c[4] * Vxx + q.c[5] * Vyy + q.c[2] * Vzz);
             // ANISO:327-352 (shear derivatives divide by the spacing)
-            if (i > 0 && j > 0) {
-                const T dVx_dy = (vx_k - ld(Vx + c - sx)) / a.dy;
-                const T dVy_dx = (vy_k - ld(Vy + c - 1)) / a.dx;
-                sxy[c] = sxy[c] * W + dt * ld(a.m[6] + c) * (dVy_dx + dVx_dy);
-            }
-            if (i > 0 && k > 0) {
-                const T dVx_dz = (vx_k - vx_m) / a.dz;
-                const T dVz_dx = (vz_k - ld(Vz + c - 1)) / a.dx;
-                sxz_new = sxz[c] * W + dt * ld(a.m[7] + c) * (dVz_dx + dVx_dz);
-                sxz[c] = sxz_new;
-            }
-            if (j > 0 && k > 0) {
-                const T dVy_dz = (vy_k - vy_m) / a.dz;
-                const T dVz_dy = (vz_k - ld(Vz + c - sx)) / a.dy;
-                syz_new = syz[c] * W + dt * ld(a.m[8] + c) * (dVy_dz + dVz_dy);
-                syz[c] = syz_new;
-            }
+            const T dVx_dy = (q.vx - q.vx_jm) / a.dy;
+            const T dVy_dx = (q.vy - q.vy_im) / a.dx;
+            sxy = q.s[3] * W + dt * q.c[6] * (dVy_dx + dVx_dy);
+            const T dVx_dz = (q.vx - vx_m) / a.dz;
+            const T dVz_dx = (vz_k - q.vz_im) / a.dx;
+            sxz = q.s[4] * W + dt * q.c[7] * (dVz_dx + dVx_dz);
+            const T dVy_dz = (q.vy - vy_m) / a.dz;
+            const T dVz_dy = (vz_k - q.vz_jm) / a.dy;
+            syz = q.s[5] * W + dt * q.c[8] * (dVy_dz + dVz_dy);
+            w_xy = (i > 0 && j > 0);
+            w_xz = (i > 0 && k > 0);
+            w_yz = (j > 0 && k > 0);
         }
+        a.f[3][c] = sxx;
+        a.f[4][c] = syy;
+        a.f[5][c] = (k == 0 && row_bc) ? T(0) : szz;
+        if (w_xy) a.f[6][c] = sxy;
+        if (w_xz) a.f[7][c] = sxz;
+        if (w_yz) a.f[8][c] = syz;
         // BC1 plane 1 from the freshly updated plane 2 (OK4:281-282)
         if (k == 2) {
-            if (i > 0 && row_bc) sxz[c - sy] = a.third * sxz_new;
-            if (j > 0) syz[c - sy] = a.third * syz_new;
+            if (i > 0 && row_bc) a.f[7][c - sy] = a.third * sxz;
+            if (j > 0) a.f[8][c - sy] = a.third * syz;
         }
-        vx_m = vx_k;
-        vy_m = vy_k;
-        vz_k = vz_p;
+        vx_m = q.vx;
+        vy_m = q.vy;
+        vz_k = q.vz_p;
     }
 }
 
@@ -201,7 +225,67 @@ __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, 
 // ---------------------------------------------------------------------------------------------
 // Velocity update.  Isotropic: OK4:346-378.  Orthorhombic: ANISO:358-389.
 // KAHAN: V = a*V + inc with the rounding error carried in comp[] (compensated summation).
+// Same structure as k_stress: hoisted, prefetched loads; predicated stores.
 // ---------------------------------------------------------------------------------------------
+template <typename T, int MODEL, bool KAHAN>
+struct VelIn {
+    T sxx, sxx_im, syy, syy_jm, szz;
+    T sxy, sxy_jp, sxy_ip;
+    T sxz_p, sxz_ip, syz_p, syz_jp;   // sxz(k+1), sxz(i+1,k), syz(k+1), syz(j+1,k)
+    T v[3];
+    T b[MODEL == MODEL_ISO ? 1 : 3];
+    T w;                              // iso: wz[k-1]; ortho: W or pz[k]
+    T cp[KAHAN ? 3 : 1];
+};
+
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, int k, VelIn<T, MODEL, KAHAN> &q)
+{
+    const int sx = a.sx;
+    const long long sy = a.sy;
+    q.sxx = ld(a.f[3] + c);
+    q.sxx_im = ld(a.f[3] + c - 1);
+    q.syy = ld(a.f[4] + c);
+    q.syy_jm = ld(a.f[4] + c - sx);
+    q.szz = ld(a.f[5] + c);
+    q.sxy = ld(a.f[6] + c);
+    q.sxy_jp = ld(a.f[6] + c + sx);
+    q.sxy_ip = ld(a.f[6] + c + 1);
+    q.sxz_p = ld(a.f[7] + c + sy);
+    q.sxz_ip = ld(a.f[7] + c + 1);
+    q.syz_p = ld(a.f[8] + c + sy);
+    q.syz_jp = ld(a.f[8] + c + sx);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) q.v[f] = a.f[f][c];
+    if (MODEL == MODEL_ISO) {
+        q.w = ld(a.w1[2] + k - 1);
+    } else {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) q.b[f] = ld(a.m[9 + f] + c);
+        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + c) : ld(a.w1[2] + k);
+    }
+    if (KAHAN) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) q.cp[f] = a.comp[f][c];
+    }
+}
+
+template <typename T, int MODEL, bool KAHAN>
+__device__ __forceinline__ T vel_update(const StepArgs<T> &a, T V, T dS, T w_or_W, T b, T &cp)
+{
+    if (!KAHAN) {
+        if (MODEL == MODEL_ISO) return w_or_W * (V * a.rdt + b * dS) * a.dt;
+        return (V * a.rdt * w_or_W + b * dS) * a.dt;
+    }
+    const T aa = w_or_W;
+    const T inc = (MODEL == MODEL_ISO) ? aa * (b * dS) * a.dt : b * dS * a.dt;
+    const T y = inc - aa * cp;
+    const T av = aa * V;
+    const T t = av + y;
+    cp = (t - av) - y;
+    return t;
+}
+
 template <typename T, int MODEL, int DAMP, bool KAHAN>
 __global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
 {
@@ -214,17 +298,7 @@ __global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
     const int sx = a.sx;
     const long long sy = a.sy;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-
-    T *__restrict__ Vx = a.f[0];
-    T *__restrict__ Vy = a.f[1];
-    T *__restrict__ Vz = a.f[2];
-    const T *__restrict__ sxx = a.f[3];
-    const T *__restrict__ syy = a.f[4];
-    const T *__restrict__ szz = a.f[5];
-    const T *__restrict__ sxy = a.f[6];
-    const T *__restrict__ sxz = a.f[7];
-    const T *__restrict__ syz = a.f[8];
-    const T dt = a.dt, rdt = a.rdt, rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
+    const T rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
 
     const bool do_x = (j < ny - 1);
     const bool do_y = (i < nx - 1);
@@ -239,76 +313,47 @@ __global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
     }
 
     long long c = (long long)i + (long long)j * sx + (long long)k0 * sy;
-    T szz_m = ld(szz + c - sy);
-    T sxz_k = ld(sxz + c);
-    T syz_k = ld(syz + c);
+    T szz_m = ld(a.f[5] + c - sy);
+    T sxz_k = ld(a.f[7] + c);
+    T syz_k = ld(a.f[8] + c);
+    VelIn<T, MODEL, KAHAN> nxt;
+    vel_load<T, MODEL, DAMP, KAHAN>(a, c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sy) {
-        const T szz_k = ld(szz + c);
-        const T sxz_p = ld(sxz + c + sy);
-        const T syz_p = ld(syz + c + sy);
-        T Wc = T(0);
-        if (MODEL == MODEL_ORTHO) {
-            if (DAMP == DAMP_W3D) Wc = ld(a.w3 + c);
-            else Wc = pxy * ld(a.w1[2] + k);
+        VelIn<T, MODEL, KAHAN> q = nxt;
+        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN>(a, c + sy, k + 1, nxt);
+        const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
+        const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
+        const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;
+        T ax, ay, az, bx, by, bz;
+        if (MODEL == MODEL_ISO) {
+            ax = wxm; ay = wym; az = q.w;
+            bx = a.bx; by = a.by; bz = a.bz;
+        } else {
+            const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
+            ax = ay = az = W;
+            bx = q.b[0]; by = q.b[1]; bz = q.b[2];
         }
+        T cpx = KAHAN ? q.cp[0] : T(0), cpy = KAHAN ? q.cp[1] : T(0), cpz = KAHAN ? q.cp[2] : T(0);
+        const T vx = vel_update<T, MODEL, KAHAN>(a, q.v[0], dSx, ax, bx, cpx);
+        const T vy = vel_update<T, MODEL, KAHAN>(a, q.v[1], dSy, ay, by, cpy);
+        const T vz = vel_update<T, MODEL, KAHAN>(a, q.v[2], dSz, az, bz, cpz);
+        // ranges OK4:358, 365, 372
         if (do_x && k < nz - 1) {
-            const T sxy_k = ld(sxy + c);
-            const T dSx = (ld(sxx + c) - ld(sxx + c - 1)) * rdx + (ld(sxy + c + sx) - sxy_k) * rdy + (sxz_p - sxz_k) * rdz;
-            T &V = Vx[c];
-            if (!KAHAN) {
-                if (MODEL == MODEL_ISO) V = wxm * (V * rdt + a.bx * dSx) * dt;
-                else V = (V * rdt * Wc + ld(a.m[9] + c) * dSx) * dt;
-            } else {
-                const T aa = (MODEL == MODEL_ISO) ? wxm : Wc;
-                const T inc = (MODEL == MODEL_ISO) ? aa * (a.bx * dSx) * dt : ld(a.m[9] + c) * dSx * dt;
-                T &cp = a.comp[0][c];
-                const T y = inc - aa * cp;
-                const T av = aa * V;
-                const T t = av + y;
-                cp = (t - av) - y;
-                V = t;
-            }
+            a.f[0][c] = vx;
+            if (KAHAN) a.comp[0][c] = cpx;
         }
         if (do_y && k < nz - 1) {
-            const T dSy = (ld(syy + c) - ld(syy + c - sx)) * rdy + (ld(sxy + c + 1) - ld(sxy + c)) * rdx + (syz_p - syz_k) * rdz;
-            T &V = Vy[c];
-            if (!KAHAN) {
-                if (MODEL == MODEL_ISO) V = wym * (V * rdt + a.by * dSy) * dt;
-                else V = (V * rdt * Wc + ld(a.m[10] + c) * dSy) * dt;
-            } else {
-                const T aa = (MODEL == MODEL_ISO) ? wym : Wc;
-                const T inc = (MODEL == MODEL_ISO) ? aa * (a.by * dSy) * dt : ld(a.m[10] + c) * dSy * dt;
-                T &cp = a.comp[1][c];
-                const T y = inc - aa * cp;
-                const T av = aa * V;
-                const T t = av + y;
-                cp = (t - av) - y;
-                V = t;
-            }
+            a.f[1][c] = vy;
+            if (KAHAN) a.comp[1][c] = cpy;
         }
         if (do_z) {
-            const T dSz = (szz_k - szz_m) * rdz + (ld(sxz + c + 1) - sxz_k) * rdx + (ld(syz + c + sx) - syz_k) * rdy;
-            T &V = Vz[c];
-            T wzm = T(0);
-            if (MODEL == MODEL_ISO) wzm = ld(a.w1[2] + k - 1);
-            if (!KAHAN) {
-                if (MODEL == MODEL_ISO) V = wzm * (V * rdt + a.bz * dSz) * dt;
-                else V = (V * rdt * Wc + ld(a.m[11] + c) * dSz) * dt;
-            } else {
-                const T aa = (MODEL == MODEL_ISO) ? wzm : Wc;
-                const T inc = (MODEL == MODEL_ISO) ? aa * (a.bz * dSz) * dt : ld(a.m[11] + c) * dSz * dt;
-                T &cp = a.comp[2][c];
-                const T y = inc - aa * cp;
-                const T av = aa * V;
-                const T t = av + y;
-                cp = (t - av) - y;
-                V = t;
-            }
+            a.f[2][c] = vz;
+            if (KAHAN) a.comp[2][c] = cpz;
         }
-        szz_m = szz_k;
-        sxz_k = sxz_p;
-        syz_k = syz_p;
+        szz_m = q.szz;
+        sxz_k = q.sxz_p;
+        syz_k = q.syz_p;
     }
 }
 
