@@ -8,6 +8,7 @@
 #include "ewfd.h"
 #include "ewfd_internal.h"
 #include "ewfd_kernels.cuh"
+#include "ewfd_fused.cuh"
 
 #include <cmath>
 #include <cstdarg>
@@ -72,6 +73,7 @@ extern "C" void ewf_params_default(ewf_params *p)
     p->damping = EWF_DAMP_PML1D;
     p->src_order = EWF_SRC_BEFORE_BC1;
     p->check_finite = 1;
+    p->fused = 0;
     p->dx = p->dy = p->dz = 1.0;
     p->dt = 1.0;
 }
@@ -153,6 +155,9 @@ struct ewf_handle {
     size_t box_elems = 0;
     long long base_off = 0;  // element offset of (0,0,0) inside an allocation
     void *f_alloc[9] = {};
+    void *g_alloc[9] = {};  // second state buffer of the fused step
+    bool fused = false;
+    int flip = 0;           // fused: the current state is in g_alloc when 1
     void *comp_alloc[3] = {};
     void *m_alloc[12] = {};
     bool m_set[12] = {};
@@ -185,12 +190,16 @@ static void *boxptr(const ewf_handle *h, void *alloc)
     return alloc ? (void *)((char *)alloc + h->base_off * (long long)h->esz) : nullptr;
 }
 
+// state buffer `which` (0: f_alloc, 1: g_alloc)
+static void *state_alloc(const ewf_handle *h, int which, int q) { return which ? h->g_alloc[q] : h->f_alloc[q]; }
+
 template <typename T>
-static StepArgs<T> make_args(const ewf_handle *h)
+static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
 {
+    if (which < 0) which = h->flip;
     StepArgs<T> a;
     memset(&a, 0, sizeof(a));
-    for (int q = 0; q < 9; ++q) a.f[q] = (T *)boxptr(h, h->f_alloc[q]);
+    for (int q = 0; q < 9; ++q) a.f[q] = (T *)boxptr(h, state_alloc(h, which, q));
     for (int q = 0; q < 3; ++q) a.comp[q] = (T *)boxptr(h, h->comp_alloc[q]);
     for (int q = 0; q < 12; ++q) a.m[q] = (const T *)boxptr(h, h->m_alloc[q]);
     for (int q = 0; q < 3; ++q) a.w1[q] = (const T *)h->w1[q];
@@ -242,6 +251,7 @@ extern "C" void ewf_destroy(ewf_handle *h)
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (auto &x : h->f_alloc) cudaFree(x);
+    for (auto &x : h->g_alloc) cudaFree(x);
     for (auto &x : h->comp_alloc) cudaFree(x);
     for (auto &x : h->m_alloc) cudaFree(x);
     for (auto &x : h->w1) cudaFree(x);
@@ -312,6 +322,7 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
     h->kchunk = p->kchunk > 0 ? p->kchunk : 16;
     h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
+    if (p->fused && (h->gsteps & 1)) h->gsteps += 1;  // fused graphs replay buffer pairs
 
 #define CKH(call)                                                                                    \
     do {                                                                                             \
@@ -332,7 +343,10 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&h->ev0));
     CKC(cudaEventCreate(&h->ev1));
+    h->fused = p->fused != 0;
     for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
+    if (h->fused)
+        for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->g_alloc[q]));
     if (p->precision == EWF_PREC_F32_KAHAN)
         for (int q = 0; q < 3; ++q) CKH(alloc_box(h, &h->comp_alloc[q]));
     for (int q = 0; q < n_materials(p->model); ++q) CKH(alloc_box(h, &h->m_alloc[q]));
@@ -387,7 +401,7 @@ extern "C" size_t ewf_field_size(const ewf_handle *h, int32_t field)
 static void *field_dev(ewf_handle *h, int id, bool *is_box)
 {
     *is_box = true;
-    if (id >= EWF_F_VX && id <= EWF_F_SYZ) return boxptr(h, h->f_alloc[id]);
+    if (id >= EWF_F_VX && id <= EWF_F_SYZ) return boxptr(h, state_alloc(h, h->flip, id));
     const int ms = material_slot(h->p.model, id);
     if (ms >= 0) return boxptr(h, h->m_alloc[ms]);
     if (id == EWF_D_W3D) return boxptr(h, h->w3_alloc);
@@ -424,6 +438,18 @@ extern "C" int ewf_set_field(ewf_handle *h, int32_t field, const void *host, siz
         else k_pack<double, double><<<nb, 256, 0, h->stream>>>((double *)dst, (const double *)h->d_stage, ex, ey, ez, sx, sy);
     }
     CK(cudaGetLastError());
+    if (h->fused && field >= EWF_F_VX && field <= EWF_F_SYZ) {
+        // both state buffers hold the cells the step never updates
+        void *dst2 = boxptr(h, state_alloc(h, 1 - h->flip, field));
+        if (h->esz == 4) {
+            if (dtype_bytes == 4) k_pack<float, float><<<nb, 256, 0, h->stream>>>((float *)dst2, (const float *)h->d_stage, ex, ey, ez, sx, sy);
+            else k_pack<float, double><<<nb, 256, 0, h->stream>>>((float *)dst2, (const double *)h->d_stage, ex, ey, ez, sx, sy);
+        } else {
+            if (dtype_bytes == 4) k_pack<double, float><<<nb, 256, 0, h->stream>>>((double *)dst2, (const float *)h->d_stage, ex, ey, ez, sx, sy);
+            else k_pack<double, double><<<nb, 256, 0, h->stream>>>((double *)dst2, (const double *)h->d_stage, ex, ey, ez, sx, sy);
+        }
+        CK(cudaGetLastError());
+    }
     CK(cudaStreamSynchronize(h->stream));
     const int ms = material_slot(h->p.model, field);
     if (ms >= 0) h->m_set[ms] = true;
@@ -480,6 +506,7 @@ extern "C" int ewf_set_stf(ewf_handle *h, const double *stf, size_t n)
 extern "C" int ewf_set_sources(ewf_handle *h, int32_t n, const int32_t *cijk, const double *coef)
 {
     if (!h || n < 0 || (n > 0 && (!cijk || !coef))) return ewf_fail(EWF_ERR_ARG, "bad source list");
+    if (n > MAXSRC) return ewf_fail(EWF_ERR_ARG, "%d point sources, at most %d", n, MAXSRC);
     std::vector<SrcEntry> v((size_t)n);
     for (int e = 0; e < n; ++e) {
         const int c = cijk[4 * e], i = cijk[4 * e + 1], j = cijk[4 * e + 2], k = cijk[4 * e + 3];
@@ -584,6 +611,8 @@ extern "C" int ewf_reset(ewf_handle *h)
 {
     if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
     for (auto x : h->f_alloc) { int s = dev_zero(h, x); if (s) return s; }
+    for (auto x : h->g_alloc) { int s = dev_zero(h, x); if (s) return s; }
+    h->flip = 0;
     for (auto x : h->comp_alloc) { int s = dev_zero(h, x); if (s) return s; }
     if (h->d_traces) CK(cudaMemsetAsync(h->d_traces, 0, (size_t)h->nrec * h->p.nt * sizeof(double), h->stream));
     CK(cudaMemsetAsync(h->d_it, 0, sizeof(int), h->stream));
@@ -612,31 +641,68 @@ static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
-typedef void (*step_fn)(const ewf_handle *, cudaEvent_t *);
+// One time step.  `parity` selects the fused step's input buffer (0: f_alloc -> g_alloc).
+typedef void (*step_fn)(const ewf_handle *, cudaEvent_t *, int parity);
 
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-static void step_entry(const ewf_handle *h, cudaEvent_t *ev)
+static void step_entry(const ewf_handle *h, cudaEvent_t *ev, int)
 {
-    const StepArgs<T> a = make_args<T>(h);
+    const StepArgs<T> a = make_args<T>(h, 0);
     launch_step_t<T, MODEL, DAMP, KAHAN>(h, a, ev);
 }
 
-static step_fn pick_step(const ewf_params &p)
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+static void fused_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
+{
+    FusedArgs<T> fa;
+    memset(&fa, 0, sizeof(fa));
+    fa.a = make_args<T>(h, parity);
+    const StepArgs<T> out = make_args<T>(h, 1 - parity);
+    for (int q = 0; q < 9; ++q) fa.o[q] = out.f[q];
+    fa.src = h->d_src;
+    fa.nsrc = h->nsrc;
+    fa.stf = h->d_stf;
+    fa.nstf = (int)h->nstf;
+    fa.it_ptr = h->d_it;
+    fa.order = h->p.src_order;
+    const dim3 blk(FX, FY);
+    const dim3 grd((h->p.nx + FX - 1) / FX, (h->p.ny + FY - 1) / FY, (h->p.nz + fa.a.kchunk - 1) / fa.a.kchunk);
+    if (ev) cudaEventRecord(ev[0], h->stream);
+    k_step<T, MODEL, DAMP, KAHAN><<<grd, blk, 0, h->stream>>>(fa);
+    if (ev) {
+        cudaEventRecord(ev[1], h->stream);
+        cudaEventRecord(ev[2], h->stream);
+        cudaEventRecord(ev[3], h->stream);
+    }
+    k_record<T><<<1, 256, 0, h->stream>>>(out, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    if (ev) cudaEventRecord(ev[4], h->stream);
+}
+
+template <bool FUSED, typename T, int MODEL, int DAMP, bool KAHAN>
+static step_fn entry()
+{
+    return FUSED ? fused_entry<T, MODEL, DAMP, KAHAN> : step_entry<T, MODEL, DAMP, KAHAN>;
+}
+
+template <bool FUSED>
+static step_fn pick_step_t(const ewf_params &p)
 {
     const bool iso = p.model == EWF_MODEL_ISO;
     const bool w3 = p.damping == EWF_DAMP_W3D;
     switch (p.precision) {
     case EWF_PREC_F32:
-        if (iso) return step_entry<float, MODEL_ISO, DAMP_PML1D, false>;
-        return w3 ? step_entry<float, MODEL_ORTHO, DAMP_W3D, false> : step_entry<float, MODEL_ORTHO, DAMP_SEP, false>;
+        if (iso) return entry<FUSED, float, MODEL_ISO, DAMP_PML1D, false>();
+        return w3 ? entry<FUSED, float, MODEL_ORTHO, DAMP_W3D, false>() : entry<FUSED, float, MODEL_ORTHO, DAMP_SEP, false>();
     case EWF_PREC_F32_KAHAN:
-        if (iso) return step_entry<float, MODEL_ISO, DAMP_PML1D, true>;
-        return w3 ? step_entry<float, MODEL_ORTHO, DAMP_W3D, true> : step_entry<float, MODEL_ORTHO, DAMP_SEP, true>;
+        if (iso) return entry<FUSED, float, MODEL_ISO, DAMP_PML1D, true>();
+        return w3 ? entry<FUSED, float, MODEL_ORTHO, DAMP_W3D, true>() : entry<FUSED, float, MODEL_ORTHO, DAMP_SEP, true>();
     default:
-        if (iso) return step_entry<double, MODEL_ISO, DAMP_PML1D, false>;
-        return w3 ? step_entry<double, MODEL_ORTHO, DAMP_W3D, false> : step_entry<double, MODEL_ORTHO, DAMP_SEP, false>;
+        if (iso) return entry<FUSED, double, MODEL_ISO, DAMP_PML1D, false>();
+        return w3 ? entry<FUSED, double, MODEL_ORTHO, DAMP_W3D, false>() : entry<FUSED, double, MODEL_ORTHO, DAMP_SEP, false>();
     }
 }
+
+static step_fn pick_step(const ewf_handle *h) { return h->fused ? pick_step_t<true>(h->p) : pick_step_t<false>(h->p); }
 
 static int inputs_ready(const ewf_handle *h)
 {
@@ -660,7 +726,7 @@ static int build_graph(ewf_handle *h, step_fn fn)
     }
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr);
+    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr, h->fused ? (s & 1) : 0);
     const cudaError_t le = cudaGetLastError();
     const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -687,14 +753,20 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
         return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
     if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf)
         return ewf_fail(EWF_ERR_ARG, "source time function has %zu samples, need %d", h->nstf, h->it + nsteps);
-    const step_fn fn = pick_step(h->p);
-    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps;
+    const step_fn fn = pick_step(h);
+    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + (h->fused ? h->flip : 0);
     if (use_graph && (h->graph_dirty || !h->gexec)) {
         st = build_graph(h, fn);
         if (st) return st;
     }
     CK(cudaEventRecord(h->ev0, h->stream));
     int done = 0;
+    int parity = h->fused ? h->flip : 0;
+    if (use_graph && parity) {  // the graph starts from buffer 0: one direct step first
+        fn(h, nullptr, parity);
+        parity = 0;
+        ++done;
+    }
     if (use_graph) {
         for (; done + h->gsteps <= nsteps; done += h->gsteps) {
             CK(cudaGraphLaunch(h->gexec, h->stream));
@@ -704,7 +776,11 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
             }
         }
     }
-    for (; done < nsteps; ++done) fn(h, nullptr);
+    for (; done < nsteps; ++done) {
+        fn(h, nullptr, parity);
+        if (h->fused) parity ^= 1;
+    }
+    h->flip = parity;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -728,13 +804,14 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     if (st) return st;
     if (h->it + nsteps > h->p.nt) return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
     if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf) return ewf_fail(EWF_ERR_ARG, "source time function too short");
-    const step_fn fn = pick_step(h->p);
+    const step_fn fn = pick_step(h);
     cudaEvent_t ev[5] = {};
     for (auto &e : ev) CK(cudaEventCreate(&e));
     double acc[4] = {0, 0, 0, 0};
     int err = EWF_OK;
     for (int s = 0; s < nsteps && !err; ++s) {
-        fn(h, ev);
+        fn(h, ev, h->flip);
+        if (h->fused) h->flip ^= 1;
         if (cudaEventSynchronize(ev[4]) != cudaSuccess) { err = ewf_fail(EWF_ERR_CUDA, "kernel timing: %s", cudaGetErrorString(cudaGetLastError())); break; }
         for (int q = 0; q < 4; ++q) {
             float ms = 0.f;
@@ -753,7 +830,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
 {
     if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *n = 3 + (h->nsrc > 0 ? 1 : 0);
+    *n = h->fused ? 2 : 3 + (h->nsrc > 0 ? 1 : 0);
     return EWF_OK;
 }
 

@@ -31,7 +31,7 @@ class Params(C.Structure):
         ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("nt", C.c_int32),
         ("model", C.c_int32), ("precision", C.c_int32), ("damping", C.c_int32), ("src_order", C.c_int32),
         ("over_y", C.c_int32), ("nout", C.c_int32), ("kchunk", C.c_int32), ("graph_steps", C.c_int32),
-        ("check_finite", C.c_int32),
+        ("check_finite", C.c_int32), ("fused", C.c_int32),
         ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
         ("c66", C.c_double), ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
         ("workdir", C.c_char_p),
@@ -122,7 +122,8 @@ class Solver:
     # -- construction --------------------------------------------------------------------
     @classmethod
     def from_model(cls, m, precision: int = F.PREC_F32, kchunk: int = 0, graph_steps: int = 0,
-                   check_finite: bool = True, damping: int | None = None, nout: int = 0) -> "Solver":
+                   check_finite: bool = True, damping: int | None = None, nout: int = 0,
+                   fused: bool | None = None) -> "Solver":
         p = default_params()
         p.nx, p.ny, p.nz, p.nt = m.nx, m.ny, m.nz, m.nt
         p.model, p.precision = m.model, precision
@@ -131,6 +132,8 @@ class Solver:
         p.kchunk, p.graph_steps, p.check_finite = kchunk, graph_steps, int(check_finite)
         p.dx, p.dy, p.dz, p.dt = m.dx, m.dy, m.dz, m.dt
         p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
+        if fused is not None:
+            p.fused = int(fused)
         s = cls(p)
         try:
             s.set_model(m)

@@ -95,6 +95,7 @@ typedef struct ewf_params {
     int32_t kchunk;       /* planes per CTA of the z-marching kernels; 0 = autotuned/default */
     int32_t graph_steps;  /* steps captured per CUDA graph; 0 = default, <0 = no graph */
     int32_t check_finite; /* 1: ewf_run checks the receiver traces for NaN/Inf */
+    int32_t fused;        /* 0 (default): stress and velocity kernels; 1: one-pass step kernel (double-buffered state) */
     double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
     double c66;            /* isotropic shear modulus pa2[7] (OK4:405) */
     double bx, by, bz;     /* isotropic 1/rho pa3[0..2] (OK4:407) */
@@ -108,7 +109,7 @@ const char *ewf_strerror(int status);
 /* Text of the last error on this thread (CUDA message, file name, ...). */
 const char *ewf_last_error(void);
 
-/* Defaults: FP32, iso, PML1D, before-BC1 order, over_y 0, graph on. */
+/* Defaults: FP32, iso, PML1D, before-BC1 order, over_y 0, graph on, two-kernel step. */
 void ewf_params_default(ewf_params *p);
 
 /* Fills dx, dy, dz, dt, c66, bx, by, bz of p from p->workdir's pa1/pa2/pa3.dat (OK4:401-407)
@@ -139,7 +140,7 @@ int ewf_set_stf(ewf_handle *h, const double *stf, size_t n);
 /* Moment tensor (xx,yy,zz,xy,xz,yz) injected at the reference's stencil around cell
  * (xs,ys,zs): stencil 0 = OK4 offsets (OK4:336-342), 1 = ANISO offsets (ANISO:233-247). */
 int ewf_set_moment_tensor(ewf_handle *h, const double mt[6], int32_t xs, int32_t ys, int32_t zs, int32_t stencil);
-/* General point sources: n entries of (field id 3..8, i, j, k) and coefficients. */
+/* General point sources: n <= 64 entries of (field id 3..8, i, j, k) and coefficients. */
 int ewf_set_sources(ewf_handle *h, int32_t n, const int32_t *comp_ijk, const double *coef);
 /* Receivers: n entries of (i, j, k, field id 0..8), sampled after every velocity update. */
 int ewf_set_receivers(ewf_handle *h, int32_t n, const int32_t *ijk_comp);
@@ -160,7 +161,8 @@ int ewf_last_run_ms(const ewf_handle *h, double *ms);
 
 /* Diagnostics: advances nsteps time steps launching each kernel between CUDA events on the
  * handle's stream (no graph) and returns the average device time per launch in ms of
- * out_ms[0] stress, [1] injection, [2] velocity, [3] receiver gather. */
+ * out_ms[0] stress (the whole fused step when fused), [1] injection, [2] velocity, [3] receiver
+ * gather (0 for kernels the step does not launch). */
 int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4]);
 /* Number of kernel launches one time step issues. */
 int ewf_launches_per_step(const ewf_handle *h, int32_t *n);

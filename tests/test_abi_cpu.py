@@ -45,7 +45,8 @@ def test_abi_version_and_strerror(built_lib):
 def test_params_struct_layout(built_lib):
     p = S.default_params()
     assert p.model == F.MODEL_ISO and p.precision == F.PREC_F32 and p.check_finite == 1
-    assert C.sizeof(S.Params) == 13 * 4 + 4 + 8 * 8 + 8
+    assert p.fused == 0
+    assert C.sizeof(S.Params) == 14 * 4 + 8 * 8 + 8
 
 
 def _have_gpu():

@@ -49,31 +49,59 @@ CASES = [
 ]
 
 
+FUSED = pytest.mark.parametrize("fused", [True, False], ids=["fused", "split"])
+
+
 @pytest.mark.parametrize("name,model,damping,nx,ny,nz", CASES, ids=[c[0] for c in CASES])
 @pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
-def test_bitwise_vs_oracle(cuda_device, name, model, damping, nx, ny, nz, prec):
+@FUSED
+def test_bitwise_vs_oracle(cuda_device, name, model, damping, nx, ny, nz, prec, fused):
     m = I.random_small(model, nx, ny, nz, nt=48, seed=nx * 7 + nz, damping=damping)
     ref = O.run(m, 48, prec)
-    assert_bitwise(product(m, 48, prec), ref, name)
+    assert_bitwise(product(m, 48, prec, fused=fused), ref, name)
 
 
 @pytest.mark.parametrize("order", [F.SRC_BEFORE_BC1, F.SRC_AFTER_BC1])
 @pytest.mark.parametrize("stencil", [0, 1])
 @pytest.mark.parametrize("zs", [0, 1, 5])
-def test_source_next_to_free_surface(cuda_device, order, stencil, zs):
+@FUSED
+def test_source_next_to_free_surface(cuda_device, order, stencil, zs, fused):
     """Injection on planes 1-2 interacts with BC1 (before-BC1 order drops / propagates it)."""
     for model in (F.MODEL_ISO, F.MODEL_ORTHO):
         m = I.random_small(model, 24, 26, 18, nt=30, seed=3 + zs, src_order=order, stencil=stencil)
         m.set_moment_tensor(np.array([1.0, -0.5, 0.25, 0.7, -0.9, 1.3]), 10, 11, zs, stencil)
         ref = O.run(m, 30)
-        assert_bitwise(product(m, 30), ref, f"model {model} order {order} stencil {stencil} zs {zs}")
+        assert_bitwise(product(m, 30, fused=fused), ref, f"model {model} order {order} stencil {stencil} zs {zs}")
+
+
+@FUSED
+def test_sources_on_tile_edges(cuda_device, fused):
+    """Point sources on the cells a CTA recomputes as halo (tile borders, chunk borders), with
+    several entries on one cell, in both injection orders."""
+    for model in (F.MODEL_ISO, F.MODEL_ORTHO):
+        for order in (F.SRC_BEFORE_BC1, F.SRC_AFTER_BC1):
+            m = I.random_small(model, 70, 20, 40, nt=25, seed=17, src_order=order)
+            ent, coef = [], []
+            rng = np.random.default_rng(1)
+            for comp in range(3, 9):
+                for (i, j, k) in ((31, 7, 1), (32, 8, 2), (31, 8, 15), (32, 7, 16), (63, 15, 17), (64, 16, 1),
+                                  (1, 1, 2), (0, 0, 31)):
+                    ent.append((comp, i, j, k))
+                    coef.append(rng.normal())
+            ent = ent[:62] + [ent[0], ent[1]]
+            coef = coef[:62] + [0.5, -0.25]
+            m.sources = np.array(ent, np.int32)
+            m.source_coef = np.array(coef)
+            ref = O.run(m, 25)
+            assert_bitwise(product(m, 25, fused=fused, kchunk=16), ref, f"model {model} order {order}")
 
 
 @pytest.mark.parametrize("kchunk,graph_steps", [(4, -1), (7, 5), (16, 0), (64, 64), (5, 3)])
-def test_tiling_and_graph_do_not_change_results(cuda_device, kchunk, graph_steps):
+@FUSED
+def test_tiling_and_graph_do_not_change_results(cuda_device, kchunk, graph_steps, fused):
     m = I.random_small(F.MODEL_ORTHO, 40, 33, 29, nt=40, seed=11, damping=F.DAMP_SEPARABLE)
     ref = O.run(m, 40)
-    assert_bitwise(product(m, 40, kchunk=kchunk, graph_steps=graph_steps, chunks=[13, 20, 7]), ref)
+    assert_bitwise(product(m, 40, kchunk=kchunk, graph_steps=graph_steps, chunks=[13, 20, 7], fused=fused), ref)
 
 
 def test_workload_shapes_small(cuda_device):
