@@ -206,6 +206,9 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     a.w3 = (const T *)boxptr(h, h->w3_alloc);
     a.sy = h->sy;
     a.sx = h->sx;
+    a.R = 1;
+    a.sxs = h->sx;
+    a.sys = h->sy;
     a.nx = h->p.nx;
     a.ny = h->p.ny;
     a.nz = h->p.nz;
@@ -825,6 +828,41 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     h->it += nsteps;
     for (int q = 0; q < 4; ++q) out_ms[q] = acc[q] / nsteps;
     return EWF_OK;
+}
+
+extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
+{
+    if (!h || nsteps < 1) return ewf_fail(EWF_ERR_ARG, "bad argument");
+    int st = inputs_ready(h);
+    if (st) return st;
+    static const int cand[] = {8, 12, 16, 24, 32, 48, 64};
+    const int steps = std::min(nsteps, h->p.nt - 1);
+    if (steps < 1) return ewf_fail(EWF_ERR_ARG, "nt too small to tune");
+    if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
+    float best = 1e30f;
+    int best_k = h->kchunk;
+    for (int kc : cand) {
+        if (kc > h->p.nz && kc != cand[0]) continue;
+        h->kchunk = std::max(4, std::min(kc, h->p.nz));
+        if ((st = ewf_reset(h))) return st;
+        const step_fn fn = pick_step(h);
+        fn(h, nullptr, h->flip);  // warm
+        if (h->fused) h->flip ^= 1;
+        CK(cudaEventRecord(h->ev0, h->stream));
+        for (int s = 0; s < steps; ++s) {
+            fn(h, nullptr, h->flip);
+            if (h->fused) h->flip ^= 1;
+        }
+        CK(cudaEventRecord(h->ev1, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        if (ms < best) { best = ms; best_k = h->kchunk; }
+    }
+    h->kchunk = best_k;
+    h->graph_dirty = true;
+    if (kchunk) *kchunk = best_k;
+    return ewf_reset(h);
 }
 
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(FX * FY, 2) k_step(const FusedArgs<T> fa)
         vy_m = ld(a.f[1] + c - sy);
         vz_k = ld(a.f[2] + c);
         if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + ps);
-        stress_load<T, MODEL, DAMP>(a, c, ps, nxt);
+        stress_load<T, MODEL, DAMP, 1>(a, c, c, ps, nxt);
     }
     T szz_m = T(0), szz_mm = T(0);   // szz(p-1), szz(p-2) of the own column
     __syncthreads();                  // s_src ready
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(FX * FY, 2) k_step(const FusedArgs<T> fa)
         if (compute) {
             if (in_grid) {
                 const StressIn<T, MODEL> q = nxt;
-                if (p + 1 < nz && p + 1 <= k1) stress_load<T, MODEL, DAMP>(a, c + sy, p + 1, nxt);
+                if (p + 1 < nz && p + 1 <= k1) stress_load<T, MODEL, DAMP, 1>(a, c + sy, c + sy, p + 1, nxt);
                 const T Vxx = (q.vx_ip - q.vx) * rdx;
                 const T Vyy = (q.vy_jp - q.vy) * rdy;
                 const T Vzz = (q.vz_p - vz_k) * rdz;

@@ -38,8 +38,11 @@ struct StepArgs {
     const T *m[12];   // iso: c11 c12 | ortho: C11 C22 C33 C12 C13 C23 C66xy C55xz C44yz Bx By Bz
     const T *w1[3];   // iso: PML profiles (n+1 each) | separable: per-axis factors (n each)
     const T *w3;      // 3-D damping field (box layout)
-    long long sy;     // plane pitch, elements
-    int sx;           // row pitch, elements
+    long long sy;     // plane pitch of materials / damping, elements
+    int sx;           // row pitch of materials / damping, elements
+    int R;            // right-hand sides interleaved along x in the state arrays (1: one source)
+    int sxs;          // state row pitch (R * sx)
+    long long sys;    // state plane pitch
     int nx, ny, nz;
     int bc1_rows;     // rows j < bc1_rows get the szz / sxz free-surface rule (OK4:279-281)
     int kchunk;       // planes per CTA
@@ -74,43 +77,45 @@ struct StressIn {
     T w;                       // iso: wz[k+1]; ortho: W or pz[k]
 };
 
-template <typename T, int MODEL, int DAMP>
-__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, int k, StressIn<T, MODEL> &q)
+// c: state index (x stride R), cm: material index of the same cell
+template <typename T, int MODEL, int DAMP, int RC>
+__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k, StressIn<T, MODEL> &q)
 {
-    const int sx = a.sx;
-    const long long sy = a.sy;
+    const int R = RC ? RC : a.R;
+    const int sx = (RC == 1) ? a.sx : a.sxs;
+    const long long sy = (RC == 1) ? a.sy : a.sys;
     q.vx = ld(a.f[0] + c);
-    q.vx_ip = ld(a.f[0] + c + 1);
+    q.vx_ip = ld(a.f[0] + c + R);
     q.vx_jm = ld(a.f[0] + c - sx);
     q.vy = ld(a.f[1] + c);
     q.vy_jp = ld(a.f[1] + c + sx);
-    q.vy_im = ld(a.f[1] + c - 1);
+    q.vy_im = ld(a.f[1] + c - R);
     q.vz_p = ld(a.f[2] + c + sy);
-    q.vz_im = ld(a.f[2] + c - 1);
+    q.vz_im = ld(a.f[2] + c - R);
     q.vz_jm = ld(a.f[2] + c - sx);
 #pragma unroll
     for (int f = 0; f < 6; ++f) q.s[f] = a.f[3 + f][c];
     if (MODEL == MODEL_ISO) {
-        q.c[0] = ld(a.m[0] + c);
-        q.c[1] = ld(a.m[1] + c);
+        q.c[0] = ld(a.m[0] + cm);
+        q.c[1] = ld(a.m[1] + cm);
         q.w = ld(a.w1[2] + k + 1);
     } else {
 #pragma unroll
-        for (int f = 0; f < 9; ++f) q.c[f] = ld(a.m[f] + c);
-        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + c) : ld(a.w1[2] + k);
+        for (int f = 0; f < 9; ++f) q.c[f] = ld(a.m[f] + cm);
+        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + cm) : ld(a.w1[2] + k);
     }
 }
 
-template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
+// The column (X = i*R + r, j) over planes [k0, k1): X runs over the cells of every RHS.
+// RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
+template <typename T, int MODEL, int DAMP, int RC>
+__device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1)
 {
-    const int i = blockIdx.x * TX + threadIdx.x;
-    const int j = blockIdx.y * TY + threadIdx.y;
+    const int R = RC ? RC : a.R;
+    const int i = (RC == 1) ? X : X / R;
     if (i >= a.nx || j >= a.ny) return;
-    const int k0 = blockIdx.z * a.kchunk;
-    const int k1 = min(k0 + a.kchunk, a.nz);
-    const int sx = a.sx;
-    const long long sy = a.sy;
+    const int sxs = (RC == 1) ? a.sx : a.sxs;
+    const long long sys = (RC == 1) ? a.sy : a.sys, sy = a.sy;
     const T dt = a.dt, rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
 
     // damping factors constant along the column
@@ -125,18 +130,20 @@ __global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
     }
     const bool row_bc = (j < a.bc1_rows);
 
-    long long c = (long long)i + (long long)j * sx + (long long)k0 * sy;
-    T vx_m = ld(a.f[0] + c - sy);  // Vx(k-1)
-    T vy_m = ld(a.f[1] + c - sy);  // Vy(k-1)
-    T vz_k = ld(a.f[2] + c);       // Vz(k)
+    long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys;
+    long long cm = (RC == 1) ? c : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
+    T vx_m = ld(a.f[0] + c - sys);  // Vx(k-1)
+    T vy_m = ld(a.f[1] + c - sys);  // Vy(k-1)
+    T vz_k = ld(a.f[2] + c);        // Vz(k)
     T wz_k = T(0);
     if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + k0);
     StressIn<T, MODEL> nxt;
-    stress_load<T, MODEL, DAMP>(a, c, k0, nxt);
+    stress_load<T, MODEL, DAMP, RC>(a, c, (RC == 1) ? c : cm, k0, nxt);
 
-    for (int k = k0; k < k1; ++k, c += sy) {
+    for (int k = k0; k < k1; ++k, c += sys) {
+        if (RC != 1 && k > k0) cm += sy;
         const StressIn<T, MODEL> q = nxt;
-        if (k + 1 < k1) stress_load<T, MODEL, DAMP>(a, c + sy, k + 1, nxt);
+        if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC>(a, c + sys, (RC == 1) ? c + sys : cm + sy, k + 1, nxt);
         const T Vxx = (q.vx_ip - q.vx) * rdx;
         const T Vyy = (q.vy_jp - q.vy) * rdy;
         const T Vzz = (q.vz_p - vz_k) * rdz;
@@ -182,13 +189,21 @@ __global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
         if (w_yz) a.f[8][c] = syz;
         // BC1 plane 1 from the freshly updated plane 2 (OK4:281-282)
         if (k == 2) {
-            if (i > 0 && row_bc) a.f[7][c - sy] = a.third * sxz;
-            if (j > 0) a.f[8][c - sy] = a.third * syz;
+            if (i > 0 && row_bc) a.f[7][c - sys] = a.third * sxz;
+            if (j > 0) a.f[8][c - sys] = a.third * syz;
         }
         vx_m = q.vx;
         vy_m = q.vy;
         vz_k = q.vz_p;
     }
+}
+
+template <typename T, int MODEL, int DAMP>
+__global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
+{
+    const int k0 = blockIdx.z * a.kchunk;
+    stress_column<T, MODEL, DAMP, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+                                  min(k0 + a.kchunk, a.nz));
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -207,7 +222,7 @@ __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, 
     const T s = (T)stf[it];
     for (int e = 0; e < nsrc; ++e) {
         const SrcEntry q = src[e];
-        const long long c = (long long)q.i + (long long)q.j * a.sx + (long long)q.k * a.sy;
+        const long long c = (long long)q.i * a.R + (long long)q.j * a.sxs + (long long)q.k * a.sys;
         T *f = a.f[q.comp];
         if (order == 0) {
             const bool row_bc = q.j < a.bc1_rows;
@@ -215,7 +230,7 @@ __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, 
             const bool yz_bc = (q.comp == 8) && q.j > 0 && q.j < a.ny && q.i < a.nx;
             if ((q.comp == 5 && q.k == 0 && row_bc) || ((xz_bc || yz_bc) && q.k == 1)) continue;
             f[c] = f[c] + (T)q.coef * s;
-            if ((xz_bc || yz_bc) && q.k == 2) f[c - a.sy] = a.third * f[c];
+            if ((xz_bc || yz_bc) && q.k == 2) f[c - a.sys] = a.third * f[c];
         } else {
             f[c] = f[c] + (T)q.coef * s;
         }
@@ -238,21 +253,22 @@ struct VelIn {
     T cp[KAHAN ? 3 : 1];
 };
 
-template <typename T, int MODEL, int DAMP, bool KAHAN>
-__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, int k, VelIn<T, MODEL, KAHAN> &q)
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC>
+__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k, VelIn<T, MODEL, KAHAN> &q)
 {
-    const int sx = a.sx;
-    const long long sy = a.sy;
+    const int R = RC ? RC : a.R;
+    const int sx = (RC == 1) ? a.sx : a.sxs;
+    const long long sy = (RC == 1) ? a.sy : a.sys;
     q.sxx = ld(a.f[3] + c);
-    q.sxx_im = ld(a.f[3] + c - 1);
+    q.sxx_im = ld(a.f[3] + c - R);
     q.syy = ld(a.f[4] + c);
     q.syy_jm = ld(a.f[4] + c - sx);
     q.szz = ld(a.f[5] + c);
     q.sxy = ld(a.f[6] + c);
     q.sxy_jp = ld(a.f[6] + c + sx);
-    q.sxy_ip = ld(a.f[6] + c + 1);
+    q.sxy_ip = ld(a.f[6] + c + R);
     q.sxz_p = ld(a.f[7] + c + sy);
-    q.sxz_ip = ld(a.f[7] + c + 1);
+    q.sxz_ip = ld(a.f[7] + c + R);
     q.syz_p = ld(a.f[8] + c + sy);
     q.syz_jp = ld(a.f[8] + c + sx);
 #pragma unroll
@@ -261,8 +277,8 @@ __device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, int 
         q.w = ld(a.w1[2] + k - 1);
     } else {
 #pragma unroll
-        for (int f = 0; f < 3; ++f) q.b[f] = ld(a.m[9 + f] + c);
-        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + c) : ld(a.w1[2] + k);
+        for (int f = 0; f < 3; ++f) q.b[f] = ld(a.m[9 + f] + cm);
+        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + cm) : ld(a.w1[2] + k);
     }
     if (KAHAN) {
 #pragma unroll
@@ -286,17 +302,17 @@ __device__ __forceinline__ T vel_update(const StepArgs<T> &a, T V, T dS, T w_or_
     return t;
 }
 
-template <typename T, int MODEL, int DAMP, bool KAHAN>
-__global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC>
+__device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1)
 {
-    const int i = blockIdx.x * TX + threadIdx.x;
-    const int j = blockIdx.y * TY + threadIdx.y;
+    const int R = RC ? RC : a.R;
+    const int i = (RC == 1) ? X : X / R;
     if (i < 1 || j < 1 || i >= a.nx || j >= a.ny) return;
-    const int k0 = max(1, (int)blockIdx.z * a.kchunk);
-    const int k1 = min((int)blockIdx.z * a.kchunk + a.kchunk, a.nz);
+    const int k0 = max(1, kc0);
+    const int k1 = kc1;
     if (k0 >= k1) return;
-    const int sx = a.sx;
-    const long long sy = a.sy;
+    const int sxs = (RC == 1) ? a.sx : a.sxs;
+    const long long sys = (RC == 1) ? a.sy : a.sys, sy = a.sy;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const T rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
 
@@ -312,16 +328,18 @@ __global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
         pxy = ld(a.w1[0] + i) * ld(a.w1[1] + j);
     }
 
-    long long c = (long long)i + (long long)j * sx + (long long)k0 * sy;
-    T szz_m = ld(a.f[5] + c - sy);
+    long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys;
+    long long cm = (RC == 1) ? c : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
+    T szz_m = ld(a.f[5] + c - sys);
     T sxz_k = ld(a.f[7] + c);
     T syz_k = ld(a.f[8] + c);
     VelIn<T, MODEL, KAHAN> nxt;
-    vel_load<T, MODEL, DAMP, KAHAN>(a, c, k0, nxt);
+    vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c, (RC == 1) ? c : cm, k0, nxt);
 
-    for (int k = k0; k < k1; ++k, c += sy) {
+    for (int k = k0; k < k1; ++k, c += sys) {
+        if (RC != 1 && k > k0) cm += sy;
         VelIn<T, MODEL, KAHAN> q = nxt;
-        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN>(a, c + sy, k + 1, nxt);
+        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c + sys, (RC == 1) ? c + sys : cm + sy, k + 1, nxt);
         const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
         const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
         const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;
@@ -355,6 +373,14 @@ __global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
         sxz_k = q.sxz_p;
         syz_k = q.syz_p;
     }
+}
+
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+__global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
+{
+    const int k0 = blockIdx.z * a.kchunk;
+    velocity_column<T, MODEL, DAMP, KAHAN, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+                                           min(k0 + a.kchunk, a.nz));
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -68,6 +68,22 @@ SIGNATURES = {
     "ewf_write_snapshot": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_pack_field_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int32,
                                          C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "ewf_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "ewf_batch_create": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "ewf_batch_destroy": (None, [C.c_void_p]),
+    "ewf_batch_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t, C.c_int32]),
+    "ewf_batch_set_stf": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_size_t]),
+    "ewf_batch_set_sources": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "ewf_batch_set_moment_tensor": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int32,
+                                              C.c_int32, C.c_int32]),
+    "ewf_batch_set_receivers": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "ewf_batch_reset": (C.c_int, [C.c_void_p]),
+    "ewf_batch_run": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_batch_last_run_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "ewf_batch_get_seismograms": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),
+    "ewf_batch_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t,
+                                      C.c_int32]),
+    "ewf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "ewf_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ewf_restore": (C.c_int, [C.c_void_p, C.c_char_p]),
 }
@@ -229,6 +245,12 @@ class Solver:
         _check(self._lib.ewf_time_kernels(self._h, int(nsteps), out), "ewf_time_kernels")
         return dict(zip(("stress", "inject", "velocity", "record"), list(out)))
 
+    def autotune(self, nsteps: int = 30) -> int:
+        """Picks the fastest z-chunk by timing `nsteps` steps per candidate; resets the state."""
+        k = C.c_int32()
+        _check(self._lib.ewf_autotune(self._h, int(nsteps), C.byref(k)), "ewf_autotune")
+        return k.value
+
     def launches_per_step(self) -> int:
         n = C.c_int32()
         _check(self._lib.ewf_launches_per_step(self._h, C.byref(n)), "ewf_launches_per_step")
@@ -291,3 +313,94 @@ def run_legacy(workdir: str, nx: int, ny: int, nz: int, model: int = F.MODEL_ISO
         ms = s.run(s.params.nt)
         s.write_legacy_outputs()
     return ms
+
+
+def params_for(m, precision: int = F.PREC_F32, kchunk: int = 0) -> Params:
+    p = default_params()
+    p.nx, p.ny, p.nz, p.nt = m.nx, m.ny, m.nz, m.nt
+    p.model, p.precision, p.damping, p.src_order, p.over_y = m.model, precision, m.damping, m.src_order, m.over_y
+    p.kchunk = kchunk
+    p.dx, p.dy, p.dz, p.dt = m.dx, m.dy, m.dz, m.dt
+    p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
+    return p
+
+
+class Batch:
+    """Several problems x right-hand sides advanced together (ewf_batch_*).
+
+    ``problems`` is a list of (Model, list of (sources, coef) per RHS); every problem's receivers
+    are recorded for each of its RHS."""
+
+    def __init__(self, problems, kchunk: int = 0):
+        lib = load_library()
+        self._lib = lib
+        self.models = [m for m, _ in problems]
+        self.nrhs = [len(r) for _, r in problems]
+        n = len(problems)
+        arr = (Params * n)(*[params_for(m, kchunk=kchunk) for m in self.models])
+        rhs = (C.c_int32 * n)(*self.nrhs)
+        h = C.c_void_p()
+        _check(lib.ewf_batch_create(n, arr, rhs, C.byref(h)), "ewf_batch_create")
+        self._h = h
+        self.nt = self.models[0].nt
+        try:
+            for pid, (m, rl) in enumerate(problems):
+                for fid, a in list(m.materials.items()) + list(m.damping_arrays.items()):
+                    a = np.ascontiguousarray(a)
+                    _check(lib.ewf_batch_set_field(h, pid, fid, _ptr(a), a.size, a.itemsize), "ewf_batch_set_field")
+                stf = np.ascontiguousarray(m.stf, np.float64)
+                _check(lib.ewf_batch_set_stf(h, pid, _ptr(stf), stf.size), "ewf_batch_set_stf")
+                for r, (ent, coef) in enumerate(rl):
+                    e = np.ascontiguousarray(ent, np.int32)
+                    c = np.ascontiguousarray(coef, np.float64)
+                    _check(lib.ewf_batch_set_sources(h, pid, r, len(c), _ptr(e), _ptr(c)), "ewf_batch_set_sources")
+                if m.receivers is not None:
+                    rec = np.ascontiguousarray(m.receivers, np.int32)
+                    _check(lib.ewf_batch_set_receivers(h, pid, len(rec), _ptr(rec)), "ewf_batch_set_receivers")
+        except Exception:
+            self.close()
+            raise
+
+    def run(self, nsteps: int) -> float:
+        _check(self._lib.ewf_batch_run(self._h, int(nsteps)), "ewf_batch_run")
+        ms = C.c_double()
+        _check(self._lib.ewf_batch_last_run_ms(self._h, C.byref(ms)), "ewf_batch_last_run_ms")
+        return ms.value
+
+    def reset(self) -> None:
+        _check(self._lib.ewf_batch_reset(self._h), "ewf_batch_reset")
+
+    def autotune(self, nsteps: int = 20) -> int:
+        k = C.c_int32()
+        _check(self._lib.ewf_batch_autotune(self._h, int(nsteps), C.byref(k)), "ewf_batch_autotune")
+        return k.value
+
+    def seismograms(self, prob: int, rhs: int) -> np.ndarray:
+        m = self.models[prob]
+        n = 0 if m.receivers is None else len(m.receivers)
+        out = np.empty((n, self.nt), np.float64)
+        _check(self._lib.ewf_batch_get_seismograms(self._h, prob, rhs, _ptr(out), out.size), "ewf_batch_get_seismograms")
+        return out
+
+    def field(self, prob: int, rhs: int, fid: int) -> np.ndarray:
+        m = self.models[prob]
+        out = np.empty(F.shape(fid, m.nx, m.ny, m.nz), np.float32)
+        _check(self._lib.ewf_batch_get_field(self._h, prob, rhs, fid, _ptr(out), out.size, 4), "ewf_batch_get_field")
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.ewf_batch_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -167,6 +167,10 @@ int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4]);
 /* Number of kernel launches one time step issues. */
 int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
 
+/* Autotuner: times `nsteps` steps for each z-chunk candidate (planes per CTA) with CUDA events,
+ * keeps the fastest (returned in *kchunk, may be NULL) and resets the state. */
+int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
+
 /* Writes 0_infos.inf and 0_0_{Src,Rec,Rec_x,Rec_y,Rec_y2,Vx,Vy,Vz}.res into workdir
  * (OK4:521-532).  Rec* are the first four receivers. */
 int ewf_write_legacy_outputs(ewf_handle *h);
@@ -198,6 +202,35 @@ int ewf_pack_field_noalloc(void *dst, int32_t dst_dtype_bytes, int32_t sx, int64
 /* Checkpoint / resume: state fields, compensation, traces and step counter. */
 int ewf_checkpoint(ewf_handle *h, const char *path);
 int ewf_restore(ewf_handle *h, const char *path);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched solver (no counterpart in the reference, which runs one model and one source per
+ * process): n problems -- models of any size and family -- each with n_rhs[i] right-hand sides
+ * (independent source sets sharing the problem's model, e.g. the 6 elementary moment tensors of
+ * a moment-tensor inversion), advanced together.  Per time step one persistent launch per model
+ * family for each of the stress and velocity phases (materials read once per cell for all the
+ * problem's RHS), one injection and one receiver launch, replayed from a CUDA graph.  FP32;
+ * every problem runs the same nt; state starts at zero.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct ewf_batch ewf_batch;
+int ewf_batch_create(int32_t n, const ewf_params *p, const int32_t *n_rhs, ewf_batch **out);
+void ewf_batch_destroy(ewf_batch *b);
+/* materials and damping of problem `prob` (shared by its RHS); reference layout as ewf_set_field */
+int ewf_batch_set_field(ewf_batch *b, int32_t prob, int32_t field, const void *host, size_t n, int32_t dtype_bytes);
+int ewf_batch_set_stf(ewf_batch *b, int32_t prob, const double *stf, size_t n);
+int ewf_batch_set_sources(ewf_batch *b, int32_t prob, int32_t rhs, int32_t n, const int32_t *comp_ijk, const double *coef);
+int ewf_batch_set_moment_tensor(ewf_batch *b, int32_t prob, int32_t rhs, const double mt[6], int32_t xs, int32_t ys,
+                                int32_t zs, int32_t stencil);
+/* receivers of problem `prob`, recorded for every RHS */
+int ewf_batch_set_receivers(ewf_batch *b, int32_t prob, int32_t n, const int32_t *ijk_comp);
+int ewf_batch_reset(ewf_batch *b);
+int ewf_batch_run(ewf_batch *b, int32_t nsteps);
+int ewf_batch_last_run_ms(const ewf_batch *b, double *ms);
+/* traces of (prob, rhs): out[r*nt + it] for the problem's n_rec receivers */
+int ewf_batch_get_seismograms(ewf_batch *b, int32_t prob, int32_t rhs, double *out, size_t n);
+int ewf_batch_get_field(ewf_batch *b, int32_t prob, int32_t rhs, int32_t field, void *host, size_t n, int32_t dtype_bytes);
+/* the z-chunk autotuner over the whole batch (leaves the batch reset) */
+int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk);
 
 #ifdef __cplusplus
 }
