@@ -94,6 +94,25 @@ def mt_entries(mt, xs: int, ys: int, zs: int, stencil: int) -> tuple[np.ndarray,
     return ent, coef
 
 
+def mt_point_entries(mt, i: int, j: int, k: int) -> tuple[np.ndarray, np.ndarray]:
+    """Entries of a moment tensor (xx, yy, zz, xy, xz, yz) as one point source at the centre of
+    cell (i, j, k): the normal components there, each shear component split equally over the four
+    edges around the centre (sxy[j', i'] sits at (i' - 1/2, j' - 1/2), so the edges are
+    i' in {i, i+1}, j' in {j, j+1}; likewise sxz and syz).  Zero components are left out.  Unlike
+    the reference's stencils above, every component acts at the same point, which keeps the
+    radiation of a laterally homogeneous model symmetric about the source."""
+    xx, yy, zz, xy, xz, yz = (float(v) for v in mt)
+    e = [(F_SXX, i, j, k, xx), (F_SYY, i, j, k, yy), (F_SZZ, i, j, k, zz)]
+    for a in (0, 1):
+        for b in (0, 1):
+            e += [(F_SXY, i + a, j + b, k, 0.25 * xy), (F_SXZ, i + a, j, k + b, 0.25 * xz),
+                  (F_SYZ, i, j + a, k + b, 0.25 * yz)]
+    e = [t for t in e if t[4] != 0.0]
+    ent = np.array([t[:4] for t in e], dtype=np.int32).reshape(-1, 4)
+    coef = np.array([t[4] for t in e], dtype=np.float64)
+    return ent, coef
+
+
 # the orthorhombic reference hard-codes its tensor (FastWaveED_GPU3D_v1_9kmst_ANISO.cu:233-247)
 ANISO_LEGACY_MT = tuple(float(np.float32(v)) for v in (-0.6282, 0.9437, 0.2439, 0.4455, -0.2709, -0.2362))
 # the four legacy traces Rec, Rec_x, Rec_y, Rec_y2 (FastWaveED_GPU3D_v1.cu:383-386; ANISO:263-266)

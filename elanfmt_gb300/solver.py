@@ -84,6 +84,17 @@ SIGNATURES = {
     "ewf_batch_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t,
                                       C.c_int32]),
     "ewf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "ewf_mlp_gemm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                               C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
+    "ewf_mlp_transpose": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "ewf_mlp_gelu_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ewf_mlp_bias_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "ewf_mlp_mse_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_float, C.c_void_p, C.c_int32,
+                                   C.c_void_p]),
+    "ewf_mlp_adam": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_float,
+                               C.c_float, C.c_float, C.c_float, C.c_int32, C.c_float, C.c_void_p]),
+    "ewf_mlp_combine": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                  C.c_void_p]),
     "ewf_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p]),
     "ewf_restore": (C.c_int, [C.c_void_p, C.c_char_p]),
 }

@@ -232,6 +232,35 @@ int ewf_batch_get_field(ewf_batch *b, int32_t prob, int32_t rhs, int32_t field, 
 /* the z-chunk autotuner over the whole batch (leaves the batch reset) */
 int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk);
 
+/* ---------------------------------------------------------------------------------------------
+ * Kernels of the learned Green's-function surrogate (no counterpart in the reference).  All
+ * buffers are caller-owned device memory; bf16 = __nv_bfloat16 stored as 16-bit words; `stream`
+ * is a cudaStream_t (NULL = default).  Calls are asynchronous on the stream.
+ * ------------------------------------------------------------------------------------------- */
+/* C[M,N] = A[M,K] . B[N,K]^T (+ bias[N]); A, B bf16 row-major; tensor cores, fp32 accumulation.
+ * Optional outputs: Cf fp32, Cb bf16, pre (fp32 value before the activation); act 0 = none,
+ * 1 = GELU (erf form).  M, N multiples of 128, K a multiple of 32. */
+int ewf_mlp_gemm(const void *A, const void *B, const float *bias, float *Cf, void *Cb, float *pre, int32_t M, int32_t N,
+                 int32_t K, int32_t act, void *stream);
+/* bf16 [rows, cols] -> [cols, rows] */
+int ewf_mlp_transpose(const void *in, void *out, int32_t rows, int32_t cols, void *stream);
+/* dx = dy * GELU'(pre), bf16 out */
+int ewf_mlp_gelu_grad(const void *dy, const float *pre, void *dx, size_t n, void *stream);
+/* db[n] = sum over m of dy[m, n] */
+int ewf_mlp_bias_grad(const void *dy, float *db, int32_t M, int32_t N, void *stream);
+/* dy = 2 (y - t) * scale (bf16); part[b] = sum of (y - t)^2 over block b's elements, b < nblocks */
+int ewf_mlp_mse_grad(const float *y, const float *t, void *dy, size_t n, float scale, float *part, int32_t nblocks,
+                     void *stream);
+/* one Adam step (bias-corrected, step >= 1, decoupled weight decay folded into the gradient) on
+ * fp32 master weights w with moments m, v; refreshes the bf16 copy wb when not NULL */
+int ewf_mlp_adam(float *w, float *m, float *v, const float *g, void *wb, size_t n, float lr, float b1, float b2, float eps,
+                 int32_t step, float weight_decay, void *stream);
+/* out[m, o, t] = sum_f R[m, o, f] * G[m, f, t] for M samples (fp32): mixes the predicted
+ * fundamental traces of each sample into its moment-tensor x component traces with the sample's
+ * azimuth-dependent matrix R.  M <= 65535, nout * nin <= 2048. */
+int ewf_mlp_combine(const float *R, const float *G, float *out, int32_t M, int32_t nout, int32_t nin, int32_t T,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif
