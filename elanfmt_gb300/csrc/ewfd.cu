@@ -12,6 +12,7 @@
 
 #include <cmath>
 #include <cstdarg>
+#include <map>
 #include <mutex>
 #include <cstdio>
 #include <cstdlib>
@@ -183,6 +184,7 @@ struct ewf_handle {
     bool graph_dirty = true;
     float last_ms = 0.f;
     int kchunk = 32;
+    bool fdiv = false;  // div_spacing verified for (float) dx, dy, dz
 };
 
 static void *boxptr(const ewf_handle *h, void *alloc)
@@ -229,7 +231,61 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     a.by = (T)h->p.by;
     a.bz = (T)h->p.bz;
     a.third = (T)1.0 / (T)3.0;
+    a.fdiv = h->fdiv ? 1 : 0;
     return a;
+}
+
+// ------------------------------------------------------------------------------------------
+// device check of div_spacing: every significand of three binades of x (2^-90, 2^0, 2^99, both
+// signs) against IEEE division; the range argument in ewfd_kernels.cuh carries the result to
+// the whole range
+// ------------------------------------------------------------------------------------------
+namespace ewf {
+__global__ void k_fdiv_check(float d, float r, unsigned *bad)
+{
+    const unsigned m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= (1u << 23)) return;
+    const unsigned expo[3] = {37u, 127u, 226u};
+    unsigned nbad = 0;
+    for (int b = 0; b < 3; ++b)
+        for (unsigned sgn = 0; sgn < 2; ++sgn) {
+            const float x = __uint_as_float((sgn << 31) | (expo[b] << 23) | m);
+            if (__float_as_uint(div_spacing(x, d, r, true)) != __float_as_uint(__fdiv_rn(x, d))) ++nbad;
+        }
+    if (nbad) atomicAdd(bad, nbad);
+}
+}  // namespace ewf
+
+bool ewf_fdiv_verified(float d)
+{
+    if (!(d >= 0x1p-10f && d <= 0x1p30f)) return false;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    uint32_t bits;
+    memcpy(&bits, &d, sizeof(bits));
+    static std::mutex mu;
+    static std::map<std::pair<int, uint32_t>, bool> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(dev, bits);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    unsigned *dbad = nullptr, hbad = 1;
+    cudaStream_t st = nullptr;
+    bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&dbad, sizeof(unsigned)) == cudaSuccess &&
+              cudaMemsetAsync(dbad, 0, sizeof(unsigned), st) == cudaSuccess;
+    if (ok) {
+        k_fdiv_check<<<(1u << 23) / 256, 256, 0, st>>>(d, 1.0f / d, dbad);
+        ok = cudaGetLastError() == cudaSuccess &&
+             cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+             cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    if (dbad) cudaFree(dbad);
+    if (st) cudaStreamDestroy(st);
+    cudaGetLastError();
+    ok = ok && hbad == 0;
+    cache[key] = ok;
+    return ok;
 }
 
 static int dev_zero(ewf_handle *h, void *alloc)
@@ -347,6 +403,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     CKC(cudaEventCreate(&h->ev0));
     CKC(cudaEventCreate(&h->ev1));
     h->fused = p->fused != 0;
+    if (p->model == EWF_MODEL_ORTHO && h->esz == 4)
+        h->fdiv = ewf_fdiv_verified((float)p->dx) && ewf_fdiv_verified((float)p->dy) && ewf_fdiv_verified((float)p->dz);
     for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
     if (h->fused)
         for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->g_alloc[q]));

@@ -46,6 +46,7 @@ struct Prob {
     bool m_set[12] = {};
     bool w_set[4] = {};
     int kchunk = 16;
+    bool fdiv = false;                      // div_spacing verified for dx, dy, dz
     std::vector<int32_t> rec;               // n x (i,j,k,comp)
     std::vector<std::vector<BatchSrc>> src;  // per RHS
     std::vector<double> stf;
@@ -186,6 +187,9 @@ extern "C" int ewf_batch_create(int32_t n, const ewf_params *p, const int32_t *n
         q.p.workdir = nullptr;
         q.R = n_rhs ? n_rhs[i] : 1;
         q.kchunk = p[i].kchunk > 0 ? p[i].kchunk : 16;
+        if (q.p.model == EWF_MODEL_ORTHO)
+            q.fdiv = ewf_fdiv_verified((float)q.p.dx) && ewf_fdiv_verified((float)q.p.dy) &&
+                     ewf_fdiv_verified((float)q.p.dz);
         const int hx = 32;
         q.sx = hx + ((q.p.nx + 2 + 31) / 32) * 32;
         q.sy = (long long)q.sx * (q.p.ny + 3);
@@ -420,6 +424,7 @@ static int build_tables(ewf_batch *b)
         d.rdx = 1.0f / d.dx; d.rdy = 1.0f / d.dy; d.rdz = 1.0f / d.dz;
         d.c66 = (float)p.c66; d.bx = (float)p.bx; d.by = (float)p.by; d.bz = (float)p.bz;
         d.third = 1.0f / 3.0f;
+        d.fdiv = q.fdiv ? 1 : 0;
         bp.tiles_x = (p.nx + TX - 1) / TX;
         bp.tiles_y = (p.ny + TY - 1) / TY;
         bp.chunks = (p.nz + q.kchunk - 1) / q.kchunk;

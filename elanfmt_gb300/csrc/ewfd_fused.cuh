@@ -55,9 +55,9 @@ __device__ __forceinline__ T shr_iso(T wprod, T s, T c66dt, T d1, T r1, T d2, T 
     return wprod * (s + c66dt * (d1 * r1 + d2 * r2));        // OK4:323-329
 }
 template <typename T>
-__device__ __forceinline__ T shr_ortho(T s, T W, T dt, T c, T d1, T h1, T d2, T h2)
+__device__ __forceinline__ T shr_ortho(T s, T W, T dt, T c, T d1, T h1, T r1, T d2, T h2, T r2, bool fd)
 {
-    return s * W + dt * c * (d1 / h1 + d2 / h2);             // ANISO:330-351
+    return s * W + dt * c * (div_spacing(d1, h1, r1, fd) + div_spacing(d2, h2, r2, fd));  // ANISO:330-351
 }
 
 template <typename T, int DAMP>
@@ -117,9 +117,9 @@ __device__ T halo_sigma(const StepArgs<T> &a, int comp, int i, int j, int k)
         return shr_iso(wx * wy * wz, old, c66dt, d1, a.rdz, d2, a.rdy);
     }
     const T W = weight3<T, DAMP>(a, c, i, j, k);
-    if (comp == 6) return shr_ortho(old, W, dt, ld(a.m[6] + c), d1, a.dx, d2, a.dy);
-    if (comp == 7) return shr_ortho(old, W, dt, ld(a.m[7] + c), d1, a.dx, d2, a.dz);
-    return shr_ortho(old, W, dt, ld(a.m[8] + c), d1, a.dz, d2, a.dy);
+    if (comp == 6) return shr_ortho(old, W, dt, ld(a.m[6] + c), d1, a.dx, a.rdx, d2, a.dy, a.rdy, a.fdiv != 0);
+    if (comp == 7) return shr_ortho(old, W, dt, ld(a.m[7] + c), d1, a.dx, a.rdx, d2, a.dz, a.rdz, a.fdiv != 0);
+    return shr_ortho(old, W, dt, ld(a.m[8] + c), d1, a.dz, a.rdz, d2, a.dy, a.rdy, a.fdiv != 0);
 }
 
 // Does BC1 (OK4:279-282) overwrite stress component `comp` of cell (i,j) on plane 1?
@@ -281,9 +281,12 @@ __global__ void __launch_bounds__(FX * FY, 2) k_step(const FusedArgs<T> fa)
                     sv[0] = nrm_ortho(q.s[0], W, dt, q.c[0], q.c[3], q.c[4], Vxx, Vyy, Vzz);
                     sv[1] = nrm_ortho(q.s[1], W, dt, q.c[3], q.c[1], q.c[5], Vxx, Vyy, Vzz);
                     sv[2] = nrm_ortho(q.s[2], W, dt, q.c[4], q.c[5], q.c[2], Vxx, Vyy, Vzz);
-                    const T xy = shr_ortho(q.s[3], W, dt, q.c[6], q.vy - q.vy_im, a.dx, q.vx - q.vx_jm, a.dy);
-                    const T xz = shr_ortho(q.s[4], W, dt, q.c[7], vz_k - q.vz_im, a.dx, q.vx - vx_m, a.dz);
-                    const T yz = shr_ortho(q.s[5], W, dt, q.c[8], q.vy - vy_m, a.dz, vz_k - q.vz_jm, a.dy);
+                    const T xy = shr_ortho(q.s[3], W, dt, q.c[6], q.vy - q.vy_im, a.dx, a.rdx, q.vx - q.vx_jm, a.dy, a.rdy,
+                                         a.fdiv != 0);
+                    const T xz = shr_ortho(q.s[4], W, dt, q.c[7], vz_k - q.vz_im, a.dx, a.rdx, q.vx - vx_m, a.dz, a.rdz,
+                                         a.fdiv != 0);
+                    const T yz = shr_ortho(q.s[5], W, dt, q.c[8], q.vy - vy_m, a.dz, a.rdz, vz_k - q.vz_jm, a.dy, a.rdy,
+                                         a.fdiv != 0);
                     sv[3] = (i > 0 && j > 0) ? xy : q.s[3];
                     sv[4] = (i > 0 && p > 0) ? xz : q.s[4];
                     sv[5] = (j > 0 && p > 0) ? yz : q.s[5];

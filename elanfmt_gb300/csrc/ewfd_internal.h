@@ -12,3 +12,6 @@ const char *ewf_workdir(const ewf_handle *h);
 int ewf_nrec(const ewf_handle *h);
 int ewf_esz(const ewf_handle *h);
 const double *ewf_stf_host_copy(const ewf_handle *h, std::vector<double> &out);
+// True when div_spacing's reciprocal path (ewfd_kernels.cuh) reproduces IEEE division by the
+// float spacing d on the current device (checked once per device and value, then cached).
+bool ewf_fdiv_verified(float d);

@@ -49,6 +49,7 @@ struct StepArgs {
     T dt, rdt, dx, dy, dz, rdx, rdy, rdz;
     T c66, bx, by, bz;  // isotropic scalars (OK4:405-407)
     T third;            // (T)1/(T)3 of BC1
+    int fdiv;           // 1: div_spacing may take the reciprocal path for dx, dy, dz (verified)
 };
 
 struct SrcEntry {
@@ -58,6 +59,30 @@ struct SrcEntry {
 
 template <typename T>
 __device__ __forceinline__ T ld(const T *p) { return __ldg(p); }
+
+// ---------------------------------------------------------------------------------------------
+// Division by a grid spacing.  The orthorhombic shear terms divide velocity differences by dx,
+// dy, dz (ANISO:327-352), and six IEEE divisions per cell cost a sixth of the stress kernel's
+// time.  div_spacing returns the same correctly rounded quotient through the reciprocal with
+// Markstein's correction step (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Develop. 34(1), 1990): with r = RN(1/d),
+// q = RN(x r), the residual e = x - q d is exact in one FMA, and RN(q + e r) is the quotient.
+// For x = 0 or 2^-90 <= |x| <= 2^100 and 2^-10 <= d <= 2^30 every intermediate stays normal
+// (the residual exact), so the result scales exactly with the binade of x; the library checks
+// it against IEEE division over whole binades of x for each spacing on the device before it
+// sets `ok` (ewfd.cu, fdiv_verified).  Other x, and unverified spacings, take IEEE division.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float div_spacing(float x, float d, float r, bool ok)
+{
+    const unsigned ax = __float_as_uint(x) & 0x7fffffffu;
+    if (ok && (ax == 0u || ax - 0x12800000u <= 0x71800000u - 0x12800000u)) {  // 2^-90 .. 2^100
+        const float q = __fmul_rn(x, r);
+        const float e = __fmaf_rn(-q, d, x);
+        return e == 0.f ? q : __fmaf_rn(e, r, q);  // e = 0: q is exact (and keeps the sign of -0)
+    }
+    return __fdiv_rn(x, d);
+}
+__device__ __forceinline__ double div_spacing(double x, double d, double, bool) { return x / d; }
 
 // ---------------------------------------------------------------------------------------------
 // Stress update.  Isotropic: OK4:285-331.  Orthorhombic: ANISO:287-356.  BC1: OK4:271-283.
@@ -168,14 +193,15 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
             syy = q.s[1] * W + dt * (q.c[3] * Vxx + q.c[1] * Vyy + q.c[5] * Vzz);
             szz = q.s[2] * W + dt * (q.c[4] * Vxx + q.c[5] * Vyy + q.c[2] * Vzz);
             // ANISO:327-352 (shear derivatives divide by the spacing)
-            const T dVx_dy = (q.vx - q.vx_jm) / a.dy;
-            const T dVy_dx = (q.vy - q.vy_im) / a.dx;
+            const bool fd = a.fdiv != 0;
+            const T dVx_dy = div_spacing(q.vx - q.vx_jm, a.dy, a.rdy, fd);
+            const T dVy_dx = div_spacing(q.vy - q.vy_im, a.dx, a.rdx, fd);
             sxy = q.s[3] * W + dt * q.c[6] * (dVy_dx + dVx_dy);
-            const T dVx_dz = (q.vx - vx_m) / a.dz;
-            const T dVz_dx = (vz_k - q.vz_im) / a.dx;
+            const T dVx_dz = div_spacing(q.vx - vx_m, a.dz, a.rdz, fd);
+            const T dVz_dx = div_spacing(vz_k - q.vz_im, a.dx, a.rdx, fd);
             sxz = q.s[4] * W + dt * q.c[7] * (dVz_dx + dVx_dz);
-            const T dVy_dz = (q.vy - vy_m) / a.dz;
-            const T dVz_dy = (vz_k - q.vz_jm) / a.dy;
+            const T dVy_dz = div_spacing(q.vy - vy_m, a.dz, a.rdz, fd);
+            const T dVz_dy = div_spacing(vz_k - q.vz_jm, a.dy, a.rdy, fd);
             syz = q.s[5] * W + dt * q.c[8] * (dVy_dz + dVz_dy);
             w_xy = (i > 0 && j > 0);
             w_xz = (i > 0 && k > 0);
