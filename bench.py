@@ -144,6 +144,19 @@ def ncu_traffic(kernel: str, workload_name: str):
     return None
 
 
+def max_over_ranks(x: float, dist=None) -> float:
+    """The slowest rank's value (replicas: every rank runs the whole workload; the job takes as
+    long as its slowest replica).  NCCL reduces device tensors, gloo host tensors."""
+    if dist is None or not dist.is_initialized():
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def cpu_baseline(m, seconds: float) -> dict:
     """FP64 C loop of the reference scheme (the CPU oracle) on this host's cores, bounded sample."""
     from elanfmt_gb300 import fields as F
@@ -225,6 +238,7 @@ def main():
     m, desc = workload(args.workload, args.nt, args.size)
     nt = m.nt
     s = Solver.from_model(m)
+    kchunk = s.autotune(30)   # the library's z-chunk autotuner (resets the state)
 
     for _ in range(args.warmup):
         s.reset()
@@ -240,11 +254,7 @@ def main():
         ms.append(s.run(nt))
     torch.cuda.synchronize()
     clocks = clk.stop()
-    total_ms = sum(ms)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(ms), dist)
     units = m.cells * nt * args.steps * world
     value = units / (total_ms * 1e-3) / 1e9
     launches = s.launches_per_step() * nt * args.steps
@@ -255,6 +265,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": nt, "receivers": len(m.receivers),
+                   "kchunk_autotuned": kchunk,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (working set ~%.1f GB)" % (m.cells * 4 * 21 / 1e9)},
         "gpu_launches": launches,

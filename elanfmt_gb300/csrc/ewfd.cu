@@ -893,7 +893,7 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     if (!h || nsteps < 1) return ewf_fail(EWF_ERR_ARG, "bad argument");
     int st = inputs_ready(h);
     if (st) return st;
-    static const int cand[] = {8, 12, 16, 24, 32, 48, 64};
+    static const int cand[] = {4, 6, 8, 12, 16, 24, 32, 48, 64};
     const int steps = std::min(nsteps, h->p.nt - 1);
     if (steps < 1) return ewf_fail(EWF_ERR_ARG, "nt too small to tune");
     if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
