@@ -97,7 +97,7 @@ bool ewf_field_extent(const ewf_params &p, int id, int *ex, int *ey, int *ez)
     case EWF_F_SYZ: case EWF_M_C44YZ: y = ny + 1; z = nz + 1; break;
     case EWF_M_C11: case EWF_M_C12: break;
     case EWF_M_C22: case EWF_M_C33: case EWF_M_C13: case EWF_M_C23:
-        if (p.model != EWF_MODEL_ORTHO) return false;
+        if (p.model != EWF_MODEL_ORTHO) return false;  // the 9 km scheme has c11/c12 only
         break;
     case EWF_D_WX: x = nx + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
     case EWF_D_WY: x = ny + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
@@ -106,7 +106,7 @@ bool ewf_field_extent(const ewf_params &p, int id, int *ex, int *ey, int *ez)
     default: return false;
     }
     if ((id == EWF_M_C66XY || id == EWF_M_C55XZ || id == EWF_M_C44YZ || id == EWF_M_BX || id == EWF_M_BY ||
-         id == EWF_M_BZ) && p.model != EWF_MODEL_ORTHO)
+         id == EWF_M_BZ) && p.model == EWF_MODEL_ISO)
         return false;
     if ((id == EWF_D_WX || id == EWF_D_WY || id == EWF_D_WZ) && p.damping == EWF_DAMP_W3D) return false;
     if (id == EWF_D_W3D && p.damping != EWF_DAMP_W3D) return false;
@@ -122,6 +122,8 @@ static int material_slot(int model, int id)
         if (id == EWF_M_C12) return 1;
         return -1;
     }
+    if (model == EWF_MODEL_ISO_HET && (id == EWF_M_C22 || id == EWF_M_C33 || id == EWF_M_C13 || id == EWF_M_C23))
+        return -1;
     switch (id) {
     case EWF_M_C11: return 0;
     case EWF_M_C22: return 1;
@@ -140,6 +142,12 @@ static int material_slot(int model, int id)
 }
 
 static int n_materials(int model) { return model == EWF_MODEL_ISO ? 2 : 12; }
+// does this model use material slot q (the 9 km scheme leaves C22, C33, C13, C23 out)
+static bool slot_used(int model, int q)
+{
+    if (q >= n_materials(model)) return false;
+    return !(model == EWF_MODEL_ISO_HET && (q == 1 || q == 2 || q == 4 || q == 5));
+}
 
 // ------------------------------------------------------------------------------------------
 // handle
@@ -232,6 +240,7 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     a.bz = (T)h->p.bz;
     a.third = (T)1.0 / (T)3.0;
     a.fdiv = h->fdiv ? 1 : 0;
+    a.vdamp = (T)h->p.vdamp;
     return a;
 }
 
@@ -336,12 +345,17 @@ static int validate_params(const ewf_params *p)
         return ewf_fail(EWF_ERR_ARG, "grid %dx%dx%d: every extent must be >= 4", p->nx, p->ny, p->nz);
     if ((long long)p->nx * p->ny * p->nz > (1LL << 36)) return ewf_fail(EWF_ERR_ARG, "grid too large");
     if (p->nt < 1) return ewf_fail(EWF_ERR_ARG, "nt must be >= 1 (got %d)", p->nt);
-    if (p->model != EWF_MODEL_ISO && p->model != EWF_MODEL_ORTHO) return ewf_fail(EWF_ERR_ARG, "unknown model %d", p->model);
+    if (p->model < EWF_MODEL_ISO || p->model > EWF_MODEL_ISO_HET) return ewf_fail(EWF_ERR_ARG, "unknown model %d", p->model);
     if (p->precision < EWF_PREC_F32 || p->precision > EWF_PREC_F64) return ewf_fail(EWF_ERR_ARG, "unknown precision %d", p->precision);
     if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles (damping 0)");
-    if (p->model == EWF_MODEL_ORTHO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
-        return ewf_fail(EWF_ERR_UNSUPPORTED, "the orthorhombic scheme uses a 3-D or separable weight field (damping 1 or 2)");
+    if (p->model != EWF_MODEL_ISO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "the orthorhombic and 9 km schemes use a 3-D or separable weight field (damping 1 or 2)");
+    if (p->model == EWF_MODEL_ISO_HET && p->fused)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "the one-pass step is built for models 0 and 1");
+    if (!(p->vdamp >= 0.0) || p->vdamp >= 1.0) return ewf_fail(EWF_ERR_ARG, "vdamp must be in [0, 1)");
+    if (p->vdamp != 0.0 && (p->model == EWF_MODEL_ISO || p->precision == EWF_PREC_F32_KAHAN || p->fused))
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "vdamp applies to models 1 and 2 in FP32/FP64 with the two-kernel step");
     if (p->src_order != EWF_SRC_BEFORE_BC1 && p->src_order != EWF_SRC_AFTER_BC1)
         return ewf_fail(EWF_ERR_ARG, "unknown src_order %d", p->src_order);
     if (p->over_y < 0) return ewf_fail(EWF_ERR_ARG, "over_y must be >= 0");
@@ -410,7 +424,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
         for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->g_alloc[q]));
     if (p->precision == EWF_PREC_F32_KAHAN)
         for (int q = 0; q < 3; ++q) CKH(alloc_box(h, &h->comp_alloc[q]));
-    for (int q = 0; q < n_materials(p->model); ++q) CKH(alloc_box(h, &h->m_alloc[q]));
+    for (int q = 0; q < n_materials(p->model); ++q)
+        if (slot_used(p->model, q)) CKH(alloc_box(h, &h->m_alloc[q]));
     if (p->damping == EWF_DAMP_W3D) {
         CKH(alloc_box(h, &h->w3_alloc));
     } else {
@@ -750,6 +765,16 @@ static step_fn pick_step_t(const ewf_params &p)
 {
     const bool iso = p.model == EWF_MODEL_ISO;
     const bool w3 = p.damping == EWF_DAMP_W3D;
+    if (p.model == EWF_MODEL_ISO_HET) {  // two-kernel step only (validated)
+        switch (p.precision) {
+        case EWF_PREC_F32:
+            return w3 ? step_entry<float, MODEL_ISOHET, DAMP_W3D, false> : step_entry<float, MODEL_ISOHET, DAMP_SEP, false>;
+        case EWF_PREC_F32_KAHAN:
+            return w3 ? step_entry<float, MODEL_ISOHET, DAMP_W3D, true> : step_entry<float, MODEL_ISOHET, DAMP_SEP, true>;
+        default:
+            return w3 ? step_entry<double, MODEL_ISOHET, DAMP_W3D, false> : step_entry<double, MODEL_ISOHET, DAMP_SEP, false>;
+        }
+    }
     switch (p.precision) {
     case EWF_PREC_F32:
         if (iso) return entry<FUSED, float, MODEL_ISO, DAMP_PML1D, false>();
@@ -768,7 +793,7 @@ static step_fn pick_step(const ewf_handle *h) { return h->fused ? pick_step_t<tr
 static int inputs_ready(const ewf_handle *h)
 {
     for (int q = 0; q < n_materials(h->p.model); ++q)
-        if (!h->m_set[q]) return ewf_fail(EWF_ERR_STATE, "material slot %d not set", q);
+        if (slot_used(h->p.model, q) && !h->m_set[q]) return ewf_fail(EWF_ERR_STATE, "material slot %d not set", q);
     if (h->p.damping == EWF_DAMP_W3D) {
         if (!h->w_set[3]) return ewf_fail(EWF_ERR_STATE, "3-D weights not set");
     } else {

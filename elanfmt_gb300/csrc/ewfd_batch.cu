@@ -157,6 +157,8 @@ extern "C" int ewf_batch_create(int32_t n, const ewf_params *p, const int32_t *n
         if (q.nt != p[0].nt) return ewf_fail(EWF_ERR_ARG, "problem %d: every problem of a batch runs the same nt", i);
         if ((q.model == EWF_MODEL_ISO) != (q.damping == EWF_DAMP_PML1D))
             return ewf_fail(EWF_ERR_UNSUPPORTED, "problem %d: model/damping combination", i);
+        if (q.model == EWF_MODEL_ISO_HET || q.vdamp != 0.0)
+            return ewf_fail(EWF_ERR_UNSUPPORTED, "problem %d: batches run models 0 and 1 without vdamp", i);
         if (q.nx > q.ny && q.over_y > 0) return ewf_fail(EWF_ERR_UNSUPPORTED, "problem %d: nx > ny with over_y > 0", i);
         if (n_rhs && (n_rhs[i] < 1 || n_rhs[i] > 64)) return ewf_fail(EWF_ERR_ARG, "problem %d: 1..64 right-hand sides", i);
         if (!(q.dx > 0 && q.dy > 0 && q.dz > 0 && q.dt > 0)) return ewf_fail(EWF_ERR_ARG, "problem %d: spacing/dt", i);

@@ -23,7 +23,7 @@
 
 namespace ewf {
 
-enum { MODEL_ISO = 0, MODEL_ORTHO = 1 };
+enum { MODEL_ISO = 0, MODEL_ORTHO = 1, MODEL_ISOHET = 2 };
 enum { DAMP_PML1D = 0, DAMP_W3D = 1, DAMP_SEP = 2 };
 
 // Tile of the z-marching kernels: one thread per (i,j) column, a CTA covers TX x TY columns
@@ -50,6 +50,7 @@ struct StepArgs {
     T c66, bx, by, bz;  // isotropic scalars (OK4:405-407)
     T third;            // (T)1/(T)3 of BC1
     int fdiv;           // 1: div_spacing may take the reciprocal path for dx, dy, dz (verified)
+    T vdamp;            // linear velocity damping (16 km scheme), 0 = off
 };
 
 struct SrcEntry {
@@ -98,8 +99,8 @@ struct StressIn {
     T vy, vy_jp, vy_im;        // Vy(i,j,k), Vy(j+1), Vy(i-1)
     T vz_p, vz_im, vz_jm;      // Vz(k+1), Vz(i-1,k), Vz(j-1,k)
     T s[6];                    // sxx syy szz sxy sxz syz at (i,j,k)
-    T c[MODEL == MODEL_ISO ? 2 : 9];
-    T w;                       // iso: wz[k+1]; ortho: W or pz[k]
+    T c[MODEL == MODEL_ISO ? 2 : (MODEL == MODEL_ISOHET ? 5 : 9)];
+    T w;                       // iso: wz[k+1]; ortho, iso-het: W or pz[k]
 };
 
 // c: state index (x stride R), cm: material index of the same cell
@@ -124,6 +125,12 @@ __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, l
         q.c[0] = ld(a.m[0] + cm);
         q.c[1] = ld(a.m[1] + cm);
         q.w = ld(a.w1[2] + k + 1);
+    } else if (MODEL == MODEL_ISOHET) {
+        q.c[0] = ld(a.m[0] + cm);  // c11u_het
+        q.c[1] = ld(a.m[3] + cm);  // c12u_het
+#pragma unroll
+        for (int f = 0; f < 3; ++f) q.c[2 + f] = ld(a.m[6 + f] + cm);  // c44u_het xy, xz, yz
+        q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + cm) : ld(a.w1[2] + k);
     } else {
 #pragma unroll
         for (int f = 0; f < 9; ++f) q.c[f] = ld(a.m[f] + cm);
@@ -186,6 +193,20 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
             sxz = wyj * wz_k * wxi * (q.s[4] + c66dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
             syz = wxi * wyj * wz_k * (q.s[5] + c66dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
             wz_k = q.w;
+        } else if (MODEL == MODEL_ISOHET) {
+            const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
+            const T c11 = q.c[0], c12 = q.c[1];
+            // 9kmst.cu:316-318
+            sxx = q.s[0] * W + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz);
+            syy = q.s[1] * W + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz);
+            szz = q.s[2] * W + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz);
+            // 9kmst.cu:321-325: edge shear moduli, derivatives times the reciprocal spacing
+            sxy = q.s[3] * W + q.c[2] * dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy);
+            sxz = q.s[4] * W + q.c[3] * dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz);
+            syz = q.s[5] * W + q.c[4] * dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy);
+            w_xy = (i > 0 && j > 0);
+            w_xz = (i > 0 && k > 0);
+            w_yz = (j > 0 && k > 0);
         } else {
             const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
             // ANISO:312-325 (c[]: C11 C22 C33 C12 C13 C23 C66 C55 C44)
@@ -317,7 +338,8 @@ __device__ __forceinline__ T vel_update(const StepArgs<T> &a, T V, T dS, T w_or_
 {
     if (!KAHAN) {
         if (MODEL == MODEL_ISO) return w_or_W * (V * a.rdt + b * dS) * a.dt;
-        return (V * a.rdt * w_or_W + b * dS) * a.dt;
+        const T r = (V * a.rdt * w_or_W + b * dS) * a.dt;
+        return a.vdamp != T(0) ? r - a.vdamp * V : r;  // 16kmst.cu:337-349
     }
     const T aa = w_or_W;
     const T inc = (MODEL == MODEL_ISO) ? aa * (b * dS) * a.dt : b * dS * a.dt;

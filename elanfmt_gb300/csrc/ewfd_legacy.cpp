@@ -136,14 +136,26 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
         const double bmax = std::max({(double)pa3[0], (double)pa3[1], (double)pa3[2]});
         vmax2 = cmax * bmax;
     } else {
-        static const struct { const char *file; int id; } files[] = {
+        struct LegacyFile { const char *file; int id; };
+        static const LegacyFile ortho_files[] = {
             {"vrho_x_11_hc.dat", EWF_M_BX}, {"vrho_y_11_hc.dat", EWF_M_BY}, {"vrho_z_11_hc.dat", EWF_M_BZ},
             {"C11m.dat", EWF_M_C11},        {"C22m.dat", EWF_M_C22},        {"C33m.dat", EWF_M_C33},
             {"C12m.dat", EWF_M_C12},        {"C13m.dat", EWF_M_C13},        {"C23m.dat", EWF_M_C23},
             {"C44myz.dat", EWF_M_C44YZ},    {"C55mxz.dat", EWF_M_C55XZ},    {"C66mxy.dat", EWF_M_C66XY},
         };
+        // the 9 km scheme's inputs (FastWaveED_GPU3D_v1_9kmst.cu:434-452)
+        static const LegacyFile isohet_files[] = {
+            {"vrho_x_11_hc.dat", EWF_M_BX},    {"vrho_y_11_hc.dat", EWF_M_BY},    {"vrho_z_11_hc.dat", EWF_M_BZ},
+            {"c11u_het.dat", EWF_M_C11},       {"c12u_het.dat", EWF_M_C12},       {"c44u_hetxy.dat", EWF_M_C66XY},
+            {"c44u_hetxz.dat", EWF_M_C55XZ},   {"c44u_hetyz.dat", EWF_M_C44YZ},
+        };
+        const bool isohet = p.model == EWF_MODEL_ISO_HET;
+        const LegacyFile *files = isohet ? isohet_files : ortho_files;
+        const size_t nfiles = isohet ? sizeof(isohet_files) / sizeof(isohet_files[0])
+                                     : sizeof(ortho_files) / sizeof(ortho_files[0]);
         double cmax = 0, bmax = 0;
-        for (const auto &f : files) {
+        for (size_t q = 0; q < nfiles; ++q) {
+            const LegacyFile &f = files[q];
             std::vector<float> v;
             if ((st = load_field(h, dir, f.file, f.id, &v))) return st;
             double m = 0;
@@ -155,7 +167,7 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
         if (p.damping == EWF_DAMP_W3D) {
             if ((st = load_field(h, dir, "weights.dat", EWF_D_W3D))) return st;
         } else {
-            return ewf_fail(EWF_ERR_UNSUPPORTED, "legacy orthorhombic inputs carry a 3-D weights.dat: use damping 1");
+            return ewf_fail(EWF_ERR_UNSUPPORTED, "legacy orthorhombic / 9 km inputs carry a 3-D weights.dat: use damping 1");
         }
     }
     const double courant = std::sqrt(vmax2) * dt * std::sqrt(1.0 / (dx * dx) + 1.0 / (dy * dy) + 1.0 / (dz * dz));
@@ -183,7 +195,8 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
         zsrc = 100;
         stencil = 0;
     } else {
-        // ANISO hard-codes the tensor in its source kernel (ANISO:233-247): xx yy zz xy xz yz
+        // ANISO (and the 9 km scheme, 9kmst.cu:228-246) hard-code the tensor in their source
+        // kernel (ANISO:233-247): xx yy zz xy xz yz
         const float c[6] = {-0.6282f, 0.9437f, 0.2439f, 0.4455f, -0.2709f, -0.2362f};
         for (int q = 0; q < 6; ++q) mt[q] = c[q];
         xsrc = 180;

@@ -7,7 +7,7 @@
  * (nx = 64*NBX - OVERX, OK4:29-41) or directly as --nx/--ny/--nz; everything else is read from
  * the same files and written to the same 0_infos.inf / 0_0_*.res outputs (OK4:521-532).
  *
- *   ewfd --nbx 12 --nby 12 --nbz 7 [--overx 0 ...] [--model iso|ortho] [--nt N]
+ *   ewfd --nbx 12 --nby 12 --nbz 7 [--overx 0 ...] [--model iso|ortho|isohet] [--nt N] [--vdamp C]
  *        [--precision f32|kahan|f64] [--src i,j,k] [--stencil ok4|aniso] [--mts FILE]
  *        [--receivers FILE] [--snap-every N] [--workdir DIR] [--quiet] [--no-checks]
  *
@@ -78,7 +78,15 @@ int main(int argc, char **argv)
         ARG_INT("--nx", p.nx) ARG_INT("--ny", p.ny) ARG_INT("--nz", p.nz) ARG_INT("--nt", p.nt)
         ARG_INT("--snap-every", snap_every) ARG_INT("--kchunk", p.kchunk)
 #undef ARG_INT
-        if (!strcmp(k, "--model") && v) { p.model = !strcmp(v, "ortho") ? EWF_MODEL_ORTHO : EWF_MODEL_ISO; ++a; continue; }
+        if (!strcmp(k, "--model") && v) {
+            if (!strcmp(v, "ortho")) p.model = EWF_MODEL_ORTHO;
+            else if (!strcmp(v, "isohet")) p.model = EWF_MODEL_ISO_HET; /* the 9 km station scheme */
+            else if (!strcmp(v, "iso")) p.model = EWF_MODEL_ISO;
+            else return fail(EWF_ERR_ARG, "--model iso|ortho|isohet");
+            ++a;
+            continue;
+        }
+        if (!strcmp(k, "--vdamp") && v) { p.vdamp = atof(v); ++a; continue; }
         if (!strcmp(k, "--precision") && v) {
             p.precision = !strcmp(v, "f64") ? EWF_PREC_F64 : !strcmp(v, "kahan") ? EWF_PREC_F32_KAHAN : EWF_PREC_F32;
             ++a;
@@ -98,8 +106,8 @@ int main(int argc, char **argv)
     if (p.ny <= 0 && nby > 0) p.ny = 64 * nby - overy;
     if (p.nz <= 0 && nbz > 0) p.nz = 64 * nbz - overz;
     p.over_y = overy;
-    p.damping = p.model == EWF_MODEL_ORTHO ? EWF_DAMP_W3D : EWF_DAMP_PML1D;
-    p.src_order = p.model == EWF_MODEL_ORTHO ? EWF_SRC_AFTER_BC1 : EWF_SRC_BEFORE_BC1;
+    p.damping = p.model == EWF_MODEL_ISO ? EWF_DAMP_PML1D : EWF_DAMP_W3D;
+    p.src_order = p.model == EWF_MODEL_ISO ? EWF_SRC_BEFORE_BC1 : EWF_SRC_AFTER_BC1;
     if (p.nx <= 0 || p.ny <= 0 || p.nz <= 0) {
         fprintf(stderr, "ewfd: give the grid as --nbx/--nby/--nbz [--overx..] or --nx/--ny/--nz\n");
         return 1;
@@ -107,7 +115,8 @@ int main(int argc, char **argv)
     int st = ewf_legacy_params(&p);
     if (st) return fail(st, "reading pa1/pa2/pa3.dat");
     if (!quiet) {
-        printf("\n  ewfd: staggered-grid elastic FDTD (%s, %s)\n", p.model == EWF_MODEL_ORTHO ? "orthorhombic" : "isotropic",
+        printf("\n  ewfd: staggered-grid elastic FDTD (%s, %s)\n",
+               p.model == EWF_MODEL_ORTHO ? "orthorhombic" : p.model == EWF_MODEL_ISO_HET ? "isotropic, heterogeneous mu/rho" : "isotropic",
                p.precision == EWF_PREC_F64 ? "fp64" : p.precision == EWF_PREC_F32_KAHAN ? "fp32+kahan" : "fp32");
         printf("Local size: %dx%dx%d, %d iterations\n", p.nx, p.ny, p.nz, p.nt);
     }
@@ -127,7 +136,7 @@ int main(int argc, char **argv)
             ewf_destroy(h);
             return 1;
         }
-        const int sten = stencil >= 0 ? stencil : (p.model == EWF_MODEL_ORTHO ? 1 : 0);
+        const int sten = stencil >= 0 ? stencil : (p.model == EWF_MODEL_ISO ? 0 : 1);
         if ((st = ewf_set_moment_tensor(h, mt, src[0], src[1], src[2], sten))) { ewf_destroy(h); return fail(st, "source"); }
     }
     if (rec_file) {

@@ -9,7 +9,7 @@ from __future__ import annotations
 import numpy as np
 
 # ewf_model / ewf_precision / ewf_damping / ewf_src_order
-MODEL_ISO, MODEL_ORTHO = 0, 1
+MODEL_ISO, MODEL_ORTHO, MODEL_ISO_HET = 0, 1, 2
 PREC_F32, PREC_F32_KAHAN, PREC_F64 = 0, 1, 2
 DAMP_PML1D, DAMP_W3D, DAMP_SEPARABLE = 0, 1, 2
 SRC_BEFORE_BC1, SRC_AFTER_BC1 = 0, 1
@@ -23,6 +23,11 @@ M_C11, M_C12, M_C22, M_C33, M_C13, M_C23 = 16, 17, 18, 19, 20, 21
 M_C66XY, M_C55XZ, M_C44YZ, M_BX, M_BY, M_BZ = 22, 23, 24, 25, 26, 27
 ISO_MATERIALS = (M_C11, M_C12)
 ORTHO_MATERIALS = (M_C11, M_C22, M_C33, M_C12, M_C13, M_C23, M_C66XY, M_C55XZ, M_C44YZ, M_BX, M_BY, M_BZ)
+# the 9 km station scheme: c11u_het, c12u_het, c44u_het xy/xz/yz (edge shear moduli), staggered 1/rho
+ISOHET_MATERIALS = (M_C11, M_C12, M_C66XY, M_C55XZ, M_C44YZ, M_BX, M_BY, M_BZ)
+# 16 km station scheme's linear velocity damping factor, (float)2.2 * (float)4.6729e-04 in float
+# (FastWaveED_GPU3D_v1_16kmst.cu:337-349)
+VDAMP_16KM = float(np.float32(np.float32(2.2) * np.float32(4.6729e-04)))
 # damping
 D_WX, D_WY, D_WZ, D_W3D = 32, 33, 34, 35
 
@@ -33,14 +38,18 @@ STATUS = {
     -9: "EWF_ERR_NODEVICE",
 }
 
-# legacy file names (FastWaveED_GPU3D_v1.cu:415-425, FastWaveED_GPU3D_v1_9kmst_ANISO.cu:411-456)
+# legacy file names per model (iso, ortho, iso-het): FastWaveED_GPU3D_v1.cu:415-425,
+# FastWaveED_GPU3D_v1_9kmst_ANISO.cu:411-456, FastWaveED_GPU3D_v1_9kmst.cu:434-452
 LEGACY_FILES = {
-    M_C11: ("c11u_het.dat", "C11m.dat"), M_C12: ("c12u_het.dat", "C12m.dat"),
-    M_C22: (None, "C22m.dat"), M_C33: (None, "C33m.dat"), M_C13: (None, "C13m.dat"), M_C23: (None, "C23m.dat"),
-    M_C66XY: (None, "C66mxy.dat"), M_C55XZ: (None, "C55mxz.dat"), M_C44YZ: (None, "C44myz.dat"),
-    M_BX: (None, "vrho_x_11_hc.dat"), M_BY: (None, "vrho_y_11_hc.dat"), M_BZ: (None, "vrho_z_11_hc.dat"),
-    D_WX: ("weights_x.dat", None), D_WY: ("weights_y.dat", None), D_WZ: ("weights_z.dat", None),
-    D_W3D: (None, "weights.dat"),
+    M_C11: ("c11u_het.dat", "C11m.dat", "c11u_het.dat"), M_C12: ("c12u_het.dat", "C12m.dat", "c12u_het.dat"),
+    M_C22: (None, "C22m.dat", None), M_C33: (None, "C33m.dat", None), M_C13: (None, "C13m.dat", None),
+    M_C23: (None, "C23m.dat", None),
+    M_C66XY: (None, "C66mxy.dat", "c44u_hetxy.dat"), M_C55XZ: (None, "C55mxz.dat", "c44u_hetxz.dat"),
+    M_C44YZ: (None, "C44myz.dat", "c44u_hetyz.dat"),
+    M_BX: (None, "vrho_x_11_hc.dat", "vrho_x_11_hc.dat"), M_BY: (None, "vrho_y_11_hc.dat", "vrho_y_11_hc.dat"),
+    M_BZ: (None, "vrho_z_11_hc.dat", "vrho_z_11_hc.dat"),
+    D_WX: ("weights_x.dat", None, None), D_WY: ("weights_y.dat", None, None), D_WZ: ("weights_z.dat", None, None),
+    D_W3D: (None, "weights.dat", "weights.dat"),
 }
 
 
@@ -115,6 +124,9 @@ def mt_point_entries(mt, i: int, j: int, k: int) -> tuple[np.ndarray, np.ndarray
 
 # the orthorhombic reference hard-codes its tensor (FastWaveED_GPU3D_v1_9kmst_ANISO.cu:233-247)
 ANISO_LEGACY_MT = tuple(float(np.float32(v)) for v in (-0.6282, 0.9437, 0.2439, 0.4455, -0.2709, -0.2362))
+# the 16 km station solver hard-codes another tensor in the same kernel and stencil
+# (FastWaveED_GPU3D_v1_16kmst.cu:228-252)
+ISO16KM_LEGACY_MT = tuple(float(np.float32(v)) for v in (-0.7448, 1.0603, 0.2439, -0.0387, -0.1953, -0.3017))
 # the four legacy traces Rec, Rec_x, Rec_y, Rec_y2 (FastWaveED_GPU3D_v1.cu:383-386; ANISO:263-266)
 OK4_LEGACY_RECEIVERS = ((504, 385, 1, F_VZ), (504, 385, 1, F_VX), (504, 388, 1, F_VY), (504, 387, 1, F_VY))
 ANISO_LEGACY_RECEIVERS = ((631, 257, 1, F_VZ), (631, 257, 1, F_VX), (631, 257, 1, F_VY), (631, 257, 1, F_VY))

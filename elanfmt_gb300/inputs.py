@@ -278,6 +278,7 @@ class Model:
     bx: float = 0.0
     by: float = 0.0
     bz: float = 0.0
+    vdamp: float = 0.0    # linear velocity damping of the 16 km scheme (0 = off)
     materials: dict = field(default_factory=dict)   # field id -> float32 array
     damping_arrays: dict = field(default_factory=dict)  # EWF_D_* -> float32 array
     sources: np.ndarray | None = None   # (n, 4) int32: comp, i, j, k
@@ -301,7 +302,7 @@ class Model:
             c = float(np.max(self.materials[F.M_C11]))
             b = max(self.bx, self.by, self.bz)
         else:
-            c = max(float(np.max(self.materials[k])) for k in (F.M_C11, F.M_C22, F.M_C33))
+            c = max(float(np.max(self.materials[k])) for k in (F.M_C11, F.M_C22, F.M_C33) if k in self.materials)
             b = max(float(np.max(self.materials[k])) for k in (F.M_BX, F.M_BY, F.M_BZ))
         return math.sqrt(c * b) * self.dt * math.sqrt(1 / self.dx**2 + 1 / self.dy**2 + 1 / self.dz**2)
 
@@ -435,6 +436,26 @@ def random_small(model: int, nx: int, ny: int, nz: int, nt: int, seed: int, damp
             w[:3] = rng.uniform(0.9, 1.0, 3)
             w[-3:] = rng.uniform(0.9, 1.0, 3)
             m.damping_arrays[key] = w.astype(np.float32)
+    elif model == F.MODEL_ISO_HET:
+        m.damping = F.DAMP_W3D if damping is None else damping
+        m.src_order = F.SRC_AFTER_BC1 if src_order is None else src_order
+        m.materials[F.M_C11] = c33.astype(np.float32)
+        m.materials[F.M_C12] = (c33 - 2 * mu).astype(np.float32)
+        m.materials[F.M_C66XY] = harmonic_edges(mu, "xy")
+        m.materials[F.M_C55XZ] = harmonic_edges(mu, "xz")
+        m.materials[F.M_C44YZ] = harmonic_edges(mu, "yz")
+        b = 1.0 / rho
+        m.materials[F.M_BX] = staggered_buoyancy(b, "x")
+        m.materials[F.M_BY] = staggered_buoyancy(b, "y")
+        m.materials[F.M_BZ] = staggered_buoyancy(b, "z")
+        px, py, pz = (np.ones(n, np.float32) for n in (nx, ny, nz))
+        for p in (px, py, pz):
+            p[:3] = rng.uniform(0.9, 1.0, 3)
+            p[-3:] = rng.uniform(0.9, 1.0, 3)
+        if m.damping == F.DAMP_SEPARABLE:
+            m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY], m.damping_arrays[F.D_WZ] = px, py, pz
+        else:
+            m.damping_arrays[F.D_W3D] = separable_weights(px, py, pz) * rng.uniform(0.999, 1.0, size=(nz, ny, nx)).astype(np.float32)
     else:
         m.damping = F.DAMP_W3D if damping is None else damping
         m.src_order = F.SRC_AFTER_BC1 if src_order is None else src_order

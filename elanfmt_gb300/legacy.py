@@ -37,13 +37,13 @@ def write_inputs(m, workdir: str) -> None:
             mt[comp_to_slot[int(c)]] = v
     _w(j("MTS.dat"), mt)
     _w(j("Src.dat"), np.asarray(m.stf[: m.nt]))
-    col = 0 if m.model == F.MODEL_ISO else 1
+    col = int(m.model)
     for fid, arr in list(m.materials.items()) + list(m.damping_arrays.items()):
         name = F.LEGACY_FILES[fid][col]
         if name is None:
             raise ValueError(f"field {fid} has no legacy file for this model")
         _w(j(name), arr)
-    if m.model == F.MODEL_ORTHO and F.D_W3D not in m.damping_arrays:
+    if m.model != F.MODEL_ISO and F.D_W3D not in m.damping_arrays:
         from .inputs import separable_weights
 
         _w(j("weights.dat"), separable_weights(m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY],

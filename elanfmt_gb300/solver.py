@@ -34,6 +34,7 @@ class Params(C.Structure):
         ("check_finite", C.c_int32), ("fused", C.c_int32),
         ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
         ("c66", C.c_double), ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
+        ("vdamp", C.c_double),
         ("workdir", C.c_char_p),
     ]
 
@@ -159,6 +160,7 @@ class Solver:
         p.kchunk, p.graph_steps, p.check_finite = kchunk, graph_steps, int(check_finite)
         p.dx, p.dy, p.dz, p.dt = m.dx, m.dy, m.dz, m.dt
         p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
+        p.vdamp = getattr(m, "vdamp", 0.0)
         if fused is not None:
             p.fused = int(fused)
         s = cls(p)
@@ -176,8 +178,8 @@ class Solver:
         p = default_params()
         p.nx, p.ny, p.nz, p.nt = nx, ny, nz, nt
         p.model, p.precision = model, precision
-        p.damping = F.DAMP_W3D if model == F.MODEL_ORTHO else F.DAMP_PML1D
-        p.src_order = F.SRC_AFTER_BC1 if model == F.MODEL_ORTHO else F.SRC_BEFORE_BC1
+        p.damping = F.DAMP_PML1D if model == F.MODEL_ISO else F.DAMP_W3D
+        p.src_order = F.SRC_BEFORE_BC1 if model == F.MODEL_ISO else F.SRC_AFTER_BC1
         p.over_y, p.check_finite = over_y, int(check_finite)
         p.workdir = os.fsencode(workdir)
         _check(load_library().ewf_legacy_params(C.byref(p)), "ewf_legacy_params")
@@ -333,6 +335,7 @@ def params_for(m, precision: int = F.PREC_F32, kchunk: int = 0) -> Params:
     p.kchunk = kchunk
     p.dx, p.dy, p.dz, p.dt = m.dx, m.dy, m.dz, m.dt
     p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
+    p.vdamp = getattr(m, "vdamp", 0.0)
     return p
 
 

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define EWF_ABI_VERSION 1
+#define EWF_ABI_VERSION 2
 
 typedef enum ewf_status {
     EWF_OK = 0,
@@ -42,8 +42,13 @@ typedef enum ewf_status {
 } ewf_status;
 
 typedef enum ewf_model {
-    EWF_MODEL_ISO = 0,   /* isotropic: c11/c12 fields, scalar shear modulus and 1/rho (OK4:285-388) */
-    EWF_MODEL_ORTHO = 1  /* orthorhombic: 9 C_ij fields + staggered buoyancy (ANISO:287-389) */
+    EWF_MODEL_ISO = 0,    /* isotropic: c11/c12 fields, scalar shear modulus and 1/rho (OK4:285-388) */
+    EWF_MODEL_ORTHO = 1,  /* orthorhombic: 9 C_ij fields + staggered buoyancy (ANISO:287-389) */
+    EWF_MODEL_ISO_HET = 2 /* isotropic with heterogeneous staggered shear moduli and buoyancy, the
+                           * 9 km station scheme (FastWaveED_GPU3D_v1_9kmst.cu:287-388): c11/c12
+                           * cell fields (EWF_M_C11/C12), c44u_hetxy/xz/yz edge fields in the
+                           * EWF_M_C66XY/C55XZ/C44YZ slots, 1/rho in EWF_M_BX/BY/BZ; 3-D or separable
+                           * weights; the ANISO loop order (BC1, then the source) */
 } ewf_model;
 
 typedef enum ewf_precision {
@@ -99,6 +104,9 @@ typedef struct ewf_params {
     double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
     double c66;            /* isotropic shear modulus pa2[7] (OK4:405) */
     double bx, by, bz;     /* isotropic 1/rho pa3[0..2] (OK4:407) */
+    double vdamp;          /* linear velocity damping: V_new = update - vdamp * V_old (16 km station
+                            * scheme, FastWaveED_GPU3D_v1_16kmst.cu:337-349, vdamp = 2.2 * 4.6729e-04
+                            * in float); 0 = off.  Models 1 and 2, FP32 / FP64, two-kernel step. */
     const char *workdir;   /* legacy *.dat inputs and *.res outputs (NULL = ".") */
 } ewf_params;
 

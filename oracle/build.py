@@ -4,7 +4,8 @@
 * ``librefkernels.so`` -- the driver-API launcher for the reference's own kernels (refkernels.c).
 * ``_ref/*.cubin``     -- the reference solvers' device code compiled from the reference sources
   where they lie (only where the reference tree is present; the cubins then travel with the
-  repository copy).  Four builds: the isotropic and orthorhombic solvers, each with the
+  repository copy).  The isotropic (OK4), orthorhombic (ANISO), 9 km (isotropic with edge shear
+  moduli) and 16 km (the 9 km scheme with linear velocity damping) solvers, each with the
   reference's own flags (``-O3``, FMA contraction on: "stock") and with ``--fmad=false``
   ("exact", every operation rounded on its own, which the oracle matches bit for bit).
 
@@ -27,6 +28,8 @@ REFERENCE_ROOT = "/root/reference"
 REF_SOURCES = {
     "ok4": "src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_OK4_final/FastWaveED_GPU3D_v1.cu",
     "aniso": "src/FastWaveED_GPU3D_v1_9km_station_ANISO/FastWaveED_GPU3D_v1_9kmst_ANISO.cu",
+    "iso9km": "src/FastWaveED_GPU3D_v1_9km_station/FastWaveED_GPU3D_v1_9kmst.cu",
+    "iso16km": "src/FastWaveED_GPU3D_v1_16km_station/FastWaveED_GPU3D_v1_16kmst.cu",
 }
 # The grid defines only size the host-side constants of the reference; every kernel takes
 # nx, ny, nz as arguments, so one build serves every grid.
@@ -73,7 +76,7 @@ def build_ref_cubins(force: bool = False) -> list[str]:
             if force or _stale(out, [src]):
                 cmds.append([nv, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", f"--fmad={fmad}",
                              "-w", *REF_DEFINES, src, "-o", out])
-    with ThreadPoolExecutor(max_workers=max(1, len(cmds))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, min(8, len(cmds)))) as ex:
         list(ex.map(_run, cmds))
     return outs
 

@@ -14,6 +14,10 @@
  *   isotropic velocity update       OK4 :346-378
  *   orthorhombic stress update      ANISO :287-356
  *   orthorhombic velocity update    ANISO :358-389
+ *   isotropic stress with edge shear moduli and staggered buoyancy (the 9 km station scheme)
+ *                                   src/FastWaveED_GPU3D_v1_9km_station/FastWaveED_GPU3D_v1_9kmst.cu:287-331;
+ *                                   its velocity update is ANISO's (9kmst.cu:333-388)
+ *   linear velocity damping         src/FastWaveED_GPU3D_v1_16km_station/FastWaveED_GPU3D_v1_16kmst.cu:337-349
  *   receiver sampling               OK4 :383-386, ANISO :254-268
  *   time-loop order                 OK4 :485-505, ANISO :519-555
  *
@@ -29,12 +33,13 @@
 
 typedef struct orc_grid {
     int32_t nx, ny, nz;
-    int32_t model;     /* 0 = isotropic (OK4 scheme), 1 = orthorhombic (ANISO scheme) */
+    int32_t model;     /* 0 = isotropic (OK4 scheme), 1 = orthorhombic (ANISO scheme), 2 = 9 km scheme */
     int32_t src_order; /* 0 = injection before BC1 (OK4), 1 = after BC1 (ANISO) */
     int32_t bc1_rows;  /* rows j < bc1_rows get the szz/sxz free-surface rule (OK4:279-281 guard iy<nx) */
     double dx, dy, dz, dt;
     double c66;        /* isotropic shear modulus, scalar pa2[7] (OK4:405) */
     double bx, by, bz; /* isotropic buoyancy 1/rho, scalars pa3[0..2] (OK4:407) */
+    double vdamp;      /* linear velocity damping (16 km scheme), 0 = off */
 } orc_grid;
 
 #define OT float
@@ -49,7 +54,7 @@ typedef struct orc_grid {
 #undef OT
 #undef OSUF
 
-int orc_abi_version(void) { return 1; }
+int orc_abi_version(void) { return 2; }
 
 int orc_num_threads(void)
 {

@@ -142,6 +142,58 @@ static void OFN(stress_ortho)(const orc_grid *g, OT *const *f, const OT *const *
     }
 }
 
+/* Isotropic stress update with cell c11/c12, edge shear moduli and a 3-D weight field, the 9 km
+ * station scheme (9kmst.cu:287-331 compute_StressPrf): ANISO's structure, but the shear
+ * derivatives are multiplied by 1/d instead of divided by d.  m[] uses the orthorhombic slots:
+ * m[0] c11u_het, m[3] c12u_het, m[6..8] c44u_het xy, xz, yz. */
+static void OFN(stress_isohet)(const orc_grid *g, OT *const *f, const OT *const *m, const OT *W)
+{
+    const long nx = g->nx, ny = g->ny, nz = g->nz;
+    const OT dt = (OT)g->dt;
+    const OT rdx = (OT)1.0 / (OT)g->dx, rdy = (OT)1.0 / (OT)g->dy, rdz = (OT)1.0 / (OT)g->dz;
+    const OT *Vx = f[0], *Vy = f[1], *Vz = f[2];
+    OT *sxx = f[3], *syy = f[4], *szz = f[5], *sxy = f[6], *sxz = f[7], *syz = f[8];
+    const OT *c11 = m[0], *c12 = m[3], *mxy = m[6], *mxz = m[7], *myz = m[8];
+    long k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < nz; k++) {
+        for (long j = 0; j < ny; j++) {
+            for (long i = 0; i < nx; i++) {
+                const long c = i + nx * (j + ny * k);
+                const OT Vxx = (Vx[(i + 1) + (nx + 1) * (j + ny * k)] - Vx[i + (nx + 1) * (j + ny * k)]) * rdx;
+                const OT Vyy = (Vy[i + nx * ((j + 1) + (ny + 1) * k)] - Vy[i + nx * (j + (ny + 1) * k)]) * rdy;
+                const OT Vzz = (Vz[i + nx * (j + ny * (k + 1))] - Vz[i + nx * (j + ny * k)]) * rdz;
+                const OT Wc = W[c];
+                /* 9kmst.cu:316-318 */
+                sxx[c] = sxx[c] * Wc + dt * (c11[c] * Vxx + c12[c] * Vyy + c12[c] * Vzz);
+                syy[c] = syy[c] * Wc + dt * (c12[c] * Vxx + c11[c] * Vyy + c12[c] * Vzz);
+                szz[c] = szz[c] * Wc + dt * (c12[c] * Vxx + c12[c] * Vyy + c11[c] * Vzz);
+                /* 9kmst.cu:321 */
+                if (i > 0 && j > 0) {
+                    const long e = i + (nx + 1) * (j + (ny + 1) * k);
+                    const OT dvy = Vy[i + nx * (j + (ny + 1) * k)] - Vy[(i - 1) + nx * (j + (ny + 1) * k)];
+                    const OT dvx = Vx[i + (nx + 1) * (j + ny * k)] - Vx[i + (nx + 1) * ((j - 1) + ny * k)];
+                    sxy[e] = sxy[e] * Wc + mxy[e] * dt * (dvy * rdx + dvx * rdy);
+                }
+                /* 9kmst.cu:323 */
+                if (i > 0 && k > 0) {
+                    const long e = i + (nx + 1) * (j + ny * k);
+                    const OT dvz = Vz[i + nx * (j + ny * k)] - Vz[(i - 1) + nx * (j + ny * k)];
+                    const OT dvx = Vx[i + (nx + 1) * (j + ny * k)] - Vx[i + (nx + 1) * (j + ny * (k - 1))];
+                    sxz[e] = sxz[e] * Wc + mxz[e] * dt * (dvz * rdx + dvx * rdz);
+                }
+                /* 9kmst.cu:325 */
+                if (j > 0 && k > 0) {
+                    const long e = i + nx * (j + (ny + 1) * k);
+                    const OT dvy = Vy[i + nx * (j + (ny + 1) * k)] - Vy[i + nx * (j + (ny + 1) * (k - 1))];
+                    const OT dvz = Vz[i + nx * (j + ny * k)] - Vz[i + nx * ((j - 1) + ny * k)];
+                    syz[e] = syz[e] * Wc + myz[e] * dt * (dvy * rdz + dvz * rdy);
+                }
+            }
+        }
+    }
+}
+
 /* Free surface (OK4:271-283 / ANISO:270-285 BC1), applied after the stress update. */
 static void OFN(bc1)(const orc_grid *g, OT *const *f)
 {
@@ -195,6 +247,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
     const OT *sxx = f[3], *syy = f[4], *szz = f[5], *sxy = f[6], *sxz = f[7], *syz = f[8];
     const int iso = (g->model == 0);
     const OT bx = (OT)g->bx, by = (OT)g->by, bz = (OT)g->bz;
+    const OT vd = (OT)g->vdamp;  /* 16kmst.cu:337-349: update - vdamp * V_old */
     long k;
 #pragma omp parallel for schedule(static)
     for (k = 1; k < nz; k++) {
@@ -212,6 +265,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
                     else     { a = W[c]; }
                     if (!comp) {
                         if (iso) Vx[e] = a * (Vx[e] * rdt + bx * dSx) * dt;
+                        else if (vd != (OT)0) Vx[e] = (Vx[e] * rdt * a + m[9][e] * dSx) * dt - vd * Vx[e];
                         else     Vx[e] = (Vx[e] * rdt * a + m[9][e] * dSx) * dt;
                     } else {
                         inc = iso ? a * (bx * dSx) * dt : m[9][e] * dSx * dt;
@@ -233,6 +287,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
                     else     { a = W[c]; }
                     if (!comp) {
                         if (iso) Vy[e] = a * (Vy[e] * rdt + by * dSy) * dt;
+                        else if (vd != (OT)0) Vy[e] = (Vy[e] * rdt * a + m[10][e] * dSy) * dt - vd * Vy[e];
                         else     Vy[e] = (Vy[e] * rdt * a + m[10][e] * dSy) * dt;
                     } else {
                         inc = iso ? a * (by * dSy) * dt : m[10][e] * dSy * dt;
@@ -254,6 +309,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
                     else     { a = W[c]; }
                     if (!comp) {
                         if (iso) Vz[e] = a * (Vz[e] * rdt + bz * dSz) * dt;
+                        else if (vd != (OT)0) Vz[e] = (Vz[e] * rdt * a + m[11][e] * dSz) * dt - vd * Vz[e];
                         else     Vz[e] = (Vz[e] * rdt * a + m[11][e] * dSz) * dt;
                     } else {
                         inc = iso ? a * (bz * dSz) * dt : m[11][e] * dSz * dt;
@@ -292,7 +348,8 @@ int OFN(orc_run)(const orc_grid *g, OT *const *f, OT *const *comp, const OT *con
     if (it0 < 0 || nsteps < 0 || it0 + nsteps > nstf) return -2;
     if (nrec > 0 && it0 + nsteps > trace_len) return -3;
     if (g->model == 0 && (!w || !w[0] || !w[1] || !w[2])) return -4;
-    if (g->model == 1 && !W) return -5;
+    if (g->model != 0 && !W) return -5;
+    if (g->model < 0 || g->model > 2) return -10;
     for (int32_t s = 0; s < nsrc; s++) {
         const int id = src[4 * s];
         long px, py;
@@ -315,8 +372,9 @@ int OFN(orc_run)(const orc_grid *g, OT *const *f, OT *const *comp, const OT *con
     }
     for (int32_t s = 0; s < nsteps; s++) {
         const int it = it0 + s;
-        if (g->model == 0) OFN(stress_iso)(g, f, m, w);
-        else               OFN(stress_ortho)(g, f, m, W);
+        if (g->model == 0)      OFN(stress_iso)(g, f, m, w);
+        else if (g->model == 2) OFN(stress_isohet)(g, f, m, W);
+        else                    OFN(stress_ortho)(g, f, m, W);
         if (g->src_order == 0) OFN(inject)(g, f, nsrc, src, coef, stf, it);
         OFN(bc1)(g, f);
         if (g->src_order != 0) OFN(inject)(g, f, nsrc, src, coef, stf, it);

@@ -7,6 +7,7 @@ FastWaveED_GPU3D_v1_9kmst_ANISO.cu:391-608): allocation, the launch geometry
 (block (32,2,8), grid covering 64*NB cells per axis, :26-31, 88-89), and the loop order
   isotropic:     compute_StressPrf, BC1, update_Qxft                    (OK4:485-505)
   orthorhombic:  compute_StressOrtho, BC1, source, update_VelocityFromStress (ANISO:519-555)
+  9 km / 16 km:  compute_StressPrf, BC1, source, update_Qxft            (9kmst.cu:463-477)
 with our receivers gathered from V after each step (a read-only gather; the reference's own
 hard-coded `record` cells are left as they are).
 
@@ -58,12 +59,13 @@ def _ck(st: int, what: str) -> None:
         raise RuntimeError(f"{what}: {lib().refk_error().decode(errors='replace')}")
 
 
-def cubin(model: int, variant: str) -> str:
-    return os.path.join(HERE, "_ref", f"{'ok4' if model == F.MODEL_ISO else 'aniso'}_{variant}.cubin")
+def cubin(model: int, variant: str, vdamp: float = 0.0) -> str:
+    name = {F.MODEL_ISO: "ok4", F.MODEL_ORTHO: "aniso"}.get(model, "iso16km" if vdamp else "iso9km")
+    return os.path.join(HERE, "_ref", f"{name}_{variant}.cubin")
 
 
-def available(model: int = F.MODEL_ISO, variant: str = "exact") -> bool:
-    return os.path.exists(cubin(model, variant))
+def available(model: int = F.MODEL_ISO, variant: str = "exact", vdamp: float = 0.0) -> bool:
+    return os.path.exists(cubin(model, variant, vdamp))
 
 
 class _Args:
@@ -98,7 +100,7 @@ class RefRunner:
         torch.zeros(1, device=self.dev)
         _ck(lib().refk_init(device), "refk_init")
         mod = C.c_void_p()
-        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant)), C.byref(mod)), "refk_load")
+        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant, getattr(m, "vdamp", 0.0))), C.byref(mod)), "refk_load")
         self.mod = mod
         nx, ny, nz = m.nx, m.ny, m.nz
         self.pad = (nx + 2) * (ny + 2) + 64
@@ -197,6 +199,47 @@ class RefRunner:
                 + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5), ("i", 0)])
             self.it_pos_vel = 24 + 16 + 3 + 1
             self.k_src = None
+        elif m.model == F.MODEL_ISO_HET:
+            if m.src_order != F.SRC_AFTER_BC1:
+                raise ValueError("9 km / 16 km reference = after-BC1 injection")
+            xs, ys, zs = self._check_sources(1)
+            vd = getattr(m, "vdamp", 0.0)
+            if vd and vd != F.VDAMP_16KM:
+                raise ValueError("the 16 km reference hard-codes its damping: use fields.VDAMP_16KM")
+            coef = tuple(float(np.float32(v)) for v in self._mt_tuple())
+            if coef != (F.ISO16KM_LEGACY_MT if vd else F.ANISO_LEGACY_MT):
+                raise ValueError("the 9 km / 16 km references hard-code their tensors")
+            c11, c12, mxy, mxz, myz, BX, BY, BZ = (self._upload(m.materials[k]) for k in F.ISOHET_MATERIALS)
+            if F.D_W3D in m.damping_arrays:
+                W = self._upload(m.damping_arrays[F.D_W3D])
+            else:
+                W = self._upload(separable_weights(m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY],
+                                                   m.damping_arrays[F.D_WZ]))
+            # compute_StressPrf(Prf, 6 stresses, Vx, Vy, Vz, Qxft, Qyft, Qzft, c11u_het, c12u_het,
+            # c44u_hetxy/xz/yz, weights, dx, dy, dz, dt, 13 unused scalars, nx, ny, nz) (9kmst.cu:287)
+            self.k_stress = self._fn("_Z17compute_StressPrf")
+            self.a_stress = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 3
+                + [("p", P(x)) for x in (c11, c12, mxy, mxz, myz, W)]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 13
+                + [("i", nx), ("i", ny), ("i", nz)])
+            self.it_pos_stress = None
+            self.k_src = self._fn("_Z6source")
+            self.a_src = _Args(
+                [("p", P(d))] * 4 + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1)] + [("p", P(d))] * 2
+                + [("p", P(self.src))] + [("f", m.dx), ("f", m.dy), ("f", m.dz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)]
+                + [("f", m.dt)])
+            self.it_pos_src = 15 + 9 + 3
+            # update_Qxft(Prf, 6 stresses, Vx, Vy, Vz, Qxft..Qzold (6), vrho x/y/z, weights, dx, dy,
+            # dz, dt, 12 unused scalars, nx, ny, nz, chi) (9kmst.cu:333)
+            self.k_vel = self._fn("_Z11update_Qxft")
+            self.a_vel = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 6
+                + [("p", P(x)) for x in (BX, BY, BZ, W)]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 12
+                + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5)])
+            self.it_pos_vel = None
         else:
             if m.src_order != F.SRC_AFTER_BC1:
                 raise ValueError("orthorhombic reference = after-BC1 injection")

@@ -3,7 +3,7 @@
 Run on a machine with a CUDA GPU, from the repository root, after oracle/build.py has compiled
 the reference sources into oracle/_ref/*.cubin:
 
-    python tests/golden/make_golden.py [out_dir]
+    python tests/golden/make_golden.py [out_dir] [case ...]
 
 For each small seeded case below it replays the reference's time loop with the reference's
 kernels (oracle/refrun.py) in both builds -- "exact" (--fmad=false) and "stock" (-O3 with FMA
@@ -50,7 +50,27 @@ def case_aniso_surface():
     return m
 
 
-CASES = {"ok4": case_ok4, "ok4_surface": case_ok4_surface, "aniso": case_aniso, "aniso_surface": case_aniso_surface}
+def case_iso9km():
+    m = I.random_small(F.MODEL_ISO_HET, 14, 16, 12, nt=40, seed=105, damping=F.DAMP_W3D)
+    m.set_moment_tensor(np.array(F.ANISO_LEGACY_MT), 5, 6, 3, 1)
+    return m
+
+
+def case_iso9km_surface():
+    m = I.random_small(F.MODEL_ISO_HET, 14, 16, 12, nt=40, seed=106, damping=F.DAMP_W3D)
+    m.set_moment_tensor(np.array(F.ANISO_LEGACY_MT), 5, 6, 0, 1)
+    return m
+
+
+def case_iso16km():
+    m = I.random_small(F.MODEL_ISO_HET, 14, 16, 12, nt=40, seed=107, damping=F.DAMP_W3D)
+    m.set_moment_tensor(np.array(F.ISO16KM_LEGACY_MT), 5, 6, 3, 1)
+    m.vdamp = F.VDAMP_16KM
+    return m
+
+
+CASES = {"ok4": case_ok4, "ok4_surface": case_ok4_surface, "aniso": case_aniso, "aniso_surface": case_aniso_surface,
+         "iso9km": case_iso9km, "iso9km_surface": case_iso9km_surface, "iso16km": case_iso16km}
 
 
 def input_digest(m) -> str:
@@ -61,14 +81,18 @@ def input_digest(m) -> str:
     for a in (m.sources, m.source_coef, m.stf, m.receivers):
         h.update(np.ascontiguousarray(a).tobytes())
     h.update(np.array([m.dx, m.dy, m.dz, m.dt, m.c66, m.bx, m.by, m.bz]).tobytes())
+    if getattr(m, "vdamp", 0.0):
+        h.update(np.array([m.vdamp]).tobytes())
     return h.hexdigest()
 
 
-def main(out_dir: str) -> None:
+def main(out_dir: str, only=()) -> None:
     from oracle import refrun as R
 
     os.makedirs(out_dir, exist_ok=True)
     for name, make in CASES.items():
+        if only and name not in only:
+            continue
         m = make()
         out = {"digest": np.array(input_digest(m)), "nsteps": np.array(m.nt)}
         for variant in ("exact", "stock"):
@@ -84,4 +108,4 @@ def main(out_dir: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden"))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden"), tuple(sys.argv[2:]))

@@ -61,6 +61,46 @@ def test_bitwise_vs_oracle(cuda_device, name, model, damping, nx, ny, nz, prec, 
     assert_bitwise(product(m, 48, prec, fused=fused), ref, name)
 
 
+ISOHET_CASES = [
+    ("isohet-w3d", F.DAMP_W3D, 35, 40, 21),
+    ("isohet-sep", F.DAMP_SEPARABLE, 29, 30, 27),
+]
+
+
+@pytest.mark.parametrize("name,damping,nx,ny,nz", ISOHET_CASES, ids=[c[0] for c in ISOHET_CASES])
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
+def test_isohet_bitwise_vs_oracle(cuda_device, name, damping, nx, ny, nz, prec):
+    """The 9 km scheme (edge shear moduli, staggered buoyancy; two-kernel step only)."""
+    m = I.random_small(F.MODEL_ISO_HET, nx, ny, nz, nt=48, seed=nx * 5 + nz, damping=damping)
+    ref = O.run(m, 48, prec)
+    assert_bitwise(product(m, 48, prec), ref, name)
+
+
+@pytest.mark.parametrize("model", [F.MODEL_ORTHO, F.MODEL_ISO_HET], ids=["ortho", "isohet"])
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F64], ids=["f32", "f64"])
+def test_velocity_damping_bitwise_vs_oracle(cuda_device, model, prec):
+    """Linear velocity damping of the 16 km scheme (V -= vdamp * V_old after each update)."""
+    m = I.random_small(model, 31, 28, 22, nt=40, seed=9, damping=F.DAMP_W3D)
+    m.vdamp = F.VDAMP_16KM
+    ref = O.run(m, 40, prec)
+    assert_bitwise(product(m, 40, prec), ref, "vdamp")
+    m.vdamp = 0.0
+    undamped = O.run(m, 40, prec)
+    assert not np.array_equal(undamped.traces, ref.traces)
+
+
+def test_isohet_and_vdamp_limits(cuda_device):
+    m = I.random_small(F.MODEL_ISO_HET, 20, 20, 16, nt=10, seed=1)
+    with pytest.raises(EwfError) as e:
+        Solver.from_model(m, fused=True)
+    assert e.value.status == -8
+    m = I.random_small(F.MODEL_ISO, 20, 20, 16, nt=10, seed=1)
+    m.vdamp = 0.001
+    with pytest.raises(EwfError) as e:
+        Solver.from_model(m)
+    assert e.value.status == -8
+
+
 @pytest.mark.parametrize("order", [F.SRC_BEFORE_BC1, F.SRC_AFTER_BC1])
 @pytest.mark.parametrize("stencil", [0, 1])
 @pytest.mark.parametrize("zs", [0, 1, 5])

@@ -36,7 +36,9 @@ def edge_mask(q, shape):
 
 
 def reference(m, nsteps, variant):
-    assert R.available(m.model, variant), f"missing {R.cubin(m.model, variant)}: run oracle/build.py where the reference is"
+    vd = getattr(m, "vdamp", 0.0)
+    assert R.available(m.model, variant, vd), \
+        f"missing {R.cubin(m.model, variant, vd)}: run oracle/build.py where the reference is"
     r = R.RefRunner(m, variant)
     try:
         r.run(nsteps)
@@ -57,9 +59,20 @@ def ortho_case(nx=36, ny=40, nz=26, nt=60, seed=22, zs=8, damping=F.DAMP_W3D):
     return m
 
 
+def isohet_case(nx=36, ny=40, nz=26, nt=60, seed=23, zs=8, damping=F.DAMP_W3D, vdamp=False):
+    """The 9 km station scheme; with vdamp, the 16 km station scheme (its tensor and damping)."""
+    m = I.random_small(F.MODEL_ISO_HET, nx, ny, nz, nt=nt, seed=seed, damping=damping)
+    mt = F.ISO16KM_LEGACY_MT if vdamp else F.ANISO_LEGACY_MT
+    m.set_moment_tensor(np.array(mt), nx // 2 - 2, ny // 2 - 2, zs, 1)
+    m.vdamp = F.VDAMP_16KM if vdamp else 0.0
+    return m
+
+
 @pytest.mark.parametrize("make", [iso_case, ortho_case, lambda: iso_case(zs=1), lambda: ortho_case(zs=0),
-                                  lambda: ortho_case(damping=F.DAMP_SEPARABLE)],
-                         ids=["iso", "ortho", "iso-surface-src", "ortho-surface-src", "ortho-separable"])
+                                  lambda: ortho_case(damping=F.DAMP_SEPARABLE), isohet_case,
+                                  lambda: isohet_case(zs=0, damping=F.DAMP_SEPARABLE), lambda: isohet_case(vdamp=True)],
+                         ids=["iso", "ortho", "iso-surface-src", "ortho-surface-src", "ortho-separable", "iso9km",
+                              "iso9km-surface-separable", "iso16km"])
 def test_product_bitwise_vs_reference_exact(cuda_device, make):
     m = make()
     rf, rt = reference(m, m.nt, "exact")
@@ -76,7 +89,7 @@ def test_product_bitwise_vs_reference_exact(cuda_device, make):
     assert np.abs(rt).max() > 0
 
 
-@pytest.mark.parametrize("model", [F.MODEL_ISO, F.MODEL_ORTHO])
+@pytest.mark.parametrize("model", [F.MODEL_ISO, F.MODEL_ORTHO, F.MODEL_ISO_HET])
 def test_seismograms_vs_reference_stock_build(cuda_device, model):
     """North-star criterion: relative L2 seismogram error <= 1e-4 against the reference built with
     its own flags (FMA contraction on), after the full run."""
@@ -84,10 +97,12 @@ def test_seismograms_vs_reference_stock_build(cuda_device, model):
         m = I.iso_homogeneous(n=64, nt=400)
         c = 31
         m.set_moment_tensor(I.mt_strike_dip_rake(30, 60, 90), c, c, c, 0)
-    else:
+    elif model == F.MODEL_ORTHO:
         m = I.ortho_layered(nx=64, ny=64, nz=48, nt=400, src=(32, 32, 12), rec_coords=[8, 20, 32, 44, 56],
                             damping=F.DAMP_W3D)
         m.set_moment_tensor(np.array(F.ANISO_LEGACY_MT), 31, 31, 11, 1)
+    else:
+        m = isohet_case(nx=64, ny=64, nz=48, nt=400, seed=24, zs=11, vdamp=True)
     _, rt = reference(m, m.nt, "stock")
     with Solver.from_model(m) as s:
         s.run(m.nt)
