@@ -74,6 +74,8 @@ struct ewf_batch {
     std::vector<Prob> probs;
     std::vector<Family> fams;
     BatchProb<float> *d_all = nullptr;  // every problem, indexed by problem id
+    std::vector<BatchProb<float>> h_all;  // host copy of d_all
+    std::vector<int> mr;                  // problems with several RHS: launched on their own
     int nrhs_total = 0;
     // sources
     BatchSrc *d_src = nullptr;
@@ -431,10 +433,16 @@ static int build_tables(ewf_batch *b)
         bp.tiles_y = (p.ny + TY - 1) / TY;
         bp.chunks = (p.nz + q.kchunk - 1) / q.kchunk;
     }
-    // families and their work lists
+    // families (single-RHS problems sharing one persistent launch) and their work lists;
+    // problems with several RHS get their own launches (k_stress_mr / k_velocity_mr)
     b->fams.clear();
+    b->mr.clear();
     std::map<std::tuple<int, int, int>, int> fam_of;
     for (int i = 0; i < n; ++i) {
+        if (b->probs[i].R > 1) {
+            b->mr.push_back(i);
+            continue;
+        }
         const auto key = std::make_tuple(b->probs[i].p.model, b->probs[i].p.damping, 1);
         if (!fam_of.count(key)) {
             fam_of[key] = (int)b->fams.size();
@@ -463,6 +471,7 @@ static int build_tables(ewf_batch *b)
     }
     CK(cudaMalloc(&b->d_all, n * sizeof(BatchProb<float>)));
     for (int i = 0; i < n; ++i) all[i].item0 = 0;
+    b->h_all = all;
     CK(cudaMemcpy(b->d_all, all.data(), n * sizeof(BatchProb<float>), cudaMemcpyHostToDevice));
     // sources grouped by (problem, rhs)
     std::vector<BatchSrc> src;
@@ -532,16 +541,37 @@ static int build_tables(ewf_batch *b)
     return EWF_OK;
 }
 
+template <int MODEL, int DAMP>
+static void launch_mr_t(const BatchProb<float> &p, bool stress, cudaStream_t s)
+{
+    const dim3 grd(p.tiles_x * p.R, p.tiles_y, p.chunks);
+    if (stress)
+        k_stress_mr<float, MODEL, DAMP><<<grd, dim3(TX, TY), 0, s>>>(p.a, p.R, p.rhs_stride);
+    else
+        k_velocity_mr<float, MODEL, DAMP><<<grd, dim3(TX, TY), 0, s>>>(p.a, p.R, p.rhs_stride);
+}
+
+static void launch_mr(const ewf_batch *b, int i, bool stress, cudaStream_t s)
+{
+    const ewf_params &q = b->probs[i].p;
+    const BatchProb<float> &p = b->h_all[i];
+    if (q.model == EWF_MODEL_ISO) launch_mr_t<MODEL_ISO, DAMP_PML1D>(p, stress, s);
+    else if (q.damping == EWF_DAMP_W3D) launch_mr_t<MODEL_ORTHO, DAMP_W3D>(p, stress, s);
+    else launch_mr_t<MODEL_ORTHO, DAMP_SEP>(p, stress, s);
+}
+
 static void batch_step(ewf_batch *b, cudaEvent_t *ev)
 {
     cudaStream_t s = b->stream;
     if (ev) cudaEventRecord(ev[0], s);
+    for (int i : b->mr) launch_mr(b, i, true, s);
     for (auto &f : b->fams) launch_family(f, true, s);
     if (ev) cudaEventRecord(ev[1], s);
     if (b->d_src)
         k_binject<float><<<(b->ngroups + 127) / 128, 128, 0, s>>>(b->d_all, b->d_src, b->d_src_start, b->ngroups, b->d_stf,
                                                                   b->d_stf_off, b->d_order, b->nt, b->d_it);
     if (ev) cudaEventRecord(ev[2], s);
+    for (int i : b->mr) launch_mr(b, i, false, s);
     for (auto &f : b->fams) launch_family(f, false, s);
     if (ev) cudaEventRecord(ev[3], s);
     if (b->nrec_total)

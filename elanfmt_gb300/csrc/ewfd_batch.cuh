@@ -88,6 +88,31 @@ __global__ void __launch_bounds__(TX * TY, 4) k_bvelocity(const BatchProb<T> *__
     }
 }
 
+// One problem with R right-hand sides in separate boxes (rhs_stride elements apart), launched on
+// its own: the problem's arguments stay in the kernel's parameter space (read by the column code
+// as constant-bank operands, as in k_stress), the RHS index is the fastest part of blockIdx.x,
+// so the R CTAs of a tile are dispatched together and read the tile's material planes from HBM
+// once (the other R-1 reads hit L2).
+template <typename T, int MODEL, int DAMP>
+__global__ void __launch_bounds__(TX * TY) k_stress_mr(const StepArgs<T> a, int R, long long rhs_stride)
+{
+    const int r = blockIdx.x % R;
+    const int tx = blockIdx.x / R;
+    const int k0 = blockIdx.z * a.kchunk;
+    stress_column<T, MODEL, DAMP, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+                                        min(k0 + a.kchunk, a.nz), (long long)r * rhs_stride);
+}
+
+template <typename T, int MODEL, int DAMP>
+__global__ void __launch_bounds__(TX * TY) k_velocity_mr(const StepArgs<T> a, int R, long long rhs_stride)
+{
+    const int r = blockIdx.x % R;
+    const int tx = blockIdx.x / R;
+    const int k0 = blockIdx.z * a.kchunk;
+    velocity_column<T, MODEL, DAMP, false, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+                                                 min(k0 + a.kchunk, a.nz), (long long)r * rhs_stride);
+}
+
 // Point injection for every (problem, RHS): one thread per (problem, RHS), entries in order,
 // with the same before/after-BC1 semantics as k_inject.
 struct BatchSrc {

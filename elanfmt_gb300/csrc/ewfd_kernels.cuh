@@ -140,9 +140,12 @@ __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, l
 
 // The column (X = i*R + r, j) over planes [k0, k1): X runs over the cells of every RHS.
 // RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
-template <typename T, int MODEL, int DAMP, int RC>
-__device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1)
+// SOFF (with RC = 1): the state lives soff elements after the materials' index (one of several
+// right-hand sides in separate boxes of the same geometry).
+template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false>
+__device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1, long long soff = 0)
 {
+    constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices
     const int R = RC ? RC : a.R;
     const int i = (RC == 1) ? X : X / R;
     if (i >= a.nx || j >= a.ny) return;
@@ -162,20 +165,20 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
     }
     const bool row_bc = (j < a.bc1_rows);
 
-    long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys;
-    long long cm = (RC == 1) ? c : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
+    long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys + (SOFF ? soff : 0);
+    long long cm = !SEP ? c : (RC == 1) ? c - soff : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
     T vx_m = ld(a.f[0] + c - sys);  // Vx(k-1)
     T vy_m = ld(a.f[1] + c - sys);  // Vy(k-1)
     T vz_k = ld(a.f[2] + c);        // Vz(k)
     T wz_k = T(0);
     if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + k0);
     StressIn<T, MODEL> nxt;
-    stress_load<T, MODEL, DAMP, RC>(a, c, (RC == 1) ? c : cm, k0, nxt);
+    stress_load<T, MODEL, DAMP, RC>(a, c, SEP ? cm : c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sys) {
-        if (RC != 1 && k > k0) cm += sy;
+        if (SEP && k > k0) cm += sy;
         const StressIn<T, MODEL> q = nxt;
-        if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC>(a, c + sys, (RC == 1) ? c + sys : cm + sy, k + 1, nxt);
+        if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
         const T Vxx = (q.vx_ip - q.vx) * rdx;
         const T Vyy = (q.vy_jp - q.vy) * rdy;
         const T Vzz = (q.vz_p - vz_k) * rdz;
@@ -350,9 +353,10 @@ __device__ __forceinline__ T vel_update(const StepArgs<T> &a, T V, T dS, T w_or_
     return t;
 }
 
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC>
-__device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1)
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false>
+__device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0)
 {
+    constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices (see stress_column)
     const int R = RC ? RC : a.R;
     const int i = (RC == 1) ? X : X / R;
     if (i < 1 || j < 1 || i >= a.nx || j >= a.ny) return;
@@ -376,18 +380,18 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
         pxy = ld(a.w1[0] + i) * ld(a.w1[1] + j);
     }
 
-    long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys;
-    long long cm = (RC == 1) ? c : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
+    long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys + (SOFF ? soff : 0);
+    long long cm = !SEP ? c : (RC == 1) ? c - soff : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
     T szz_m = ld(a.f[5] + c - sys);
     T sxz_k = ld(a.f[7] + c);
     T syz_k = ld(a.f[8] + c);
     VelIn<T, MODEL, KAHAN> nxt;
-    vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c, (RC == 1) ? c : cm, k0, nxt);
+    vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c, SEP ? cm : c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sys) {
-        if (RC != 1 && k > k0) cm += sy;
+        if (SEP && k > k0) cm += sy;
         VelIn<T, MODEL, KAHAN> q = nxt;
-        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c + sys, (RC == 1) ? c + sys : cm + sy, k + 1, nxt);
+        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
         const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
         const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
         const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;
