@@ -409,6 +409,41 @@ def ortho_layered(nx: int = 320, ny: int = 320, nz: int = 256, nt: int = 4000, d
     return m
 
 
+def iso_het_layered(nx: int, ny: int, nz: int, nt: int, dx: float, dt: float, layers: list[dict],
+                    thick: int = 120, margin_y: int = 210, rate: float = 0.16) -> Model:
+    """The 9 km station driver's model (vizme_FastWaveED_GPU3D_9kmst.m:255-444) for the
+    EWF_MODEL_ISO_HET scheme.  ``layers`` = [{"top": k0, "vp": m/s, "vs": m/s, "rho": kg/m^3}, ...]
+    by increasing top (the first layer's top is 0): cell fields c11 = rho vp^2 and
+    c12 = K - 2/3 mu with K = c11 - 4/3 mu, mu = rho vs^2 (:262-268); the edge shear moduli are the
+    4-cell harmonic means of mu with zero border planes (:377-396); the staggered 1/rho fields
+    are the 2-point means with zero boundary faces (:323-350); the 3-D sponge weights.dat (:397-444,
+    sponge_3d_legacy).  Source and receivers are left to the caller."""
+    tops = [int(L["top"]) for L in layers] + [nz]
+    mu = np.empty((nz, ny, nx))
+    c11 = np.empty((nz, ny, nx))
+    rho = np.empty((nz, ny, nx))
+    for L, k0, k1 in zip(layers, tops[:-1], tops[1:]):
+        r = float(L["rho"])
+        rho[k0:k1] = r
+        c11[k0:k1] = float(L["vp"]) ** 2 * r
+        mu[k0:k1] = float(L["vs"]) ** 2 * r
+    K = c11 - 4.0 / 3.0 * mu
+    m = Model(nx=nx, ny=ny, nz=nz, nt=nt, dx=float(np.float32(dx)), dy=float(np.float32(dx)), dz=float(np.float32(dx)),
+              dt=float(np.float32(dt)), model=F.MODEL_ISO_HET, damping=F.DAMP_W3D, src_order=F.SRC_AFTER_BC1,
+              name=f"iso_het_{nx}x{ny}x{nz}")
+    m.materials[F.M_C11] = c11.astype(np.float32)
+    m.materials[F.M_C12] = (K - 2.0 / 3.0 * mu).astype(np.float32)
+    m.materials[F.M_C66XY] = harmonic_edges(mu, "xy")
+    m.materials[F.M_C55XZ] = harmonic_edges(mu, "xz")
+    m.materials[F.M_C44YZ] = harmonic_edges(mu, "yz")
+    b = 1.0 / rho
+    m.materials[F.M_BX] = staggered_buoyancy(b, "x")
+    m.materials[F.M_BY] = staggered_buoyancy(b, "y")
+    m.materials[F.M_BZ] = staggered_buoyancy(b, "z")
+    m.damping_arrays[F.D_W3D] = sponge_3d_legacy(nx, ny, nz, thick=thick, margin_y=margin_y, rate=rate)
+    return m
+
+
 def random_small(model: int, nx: int, ny: int, nz: int, nt: int, seed: int, damping: int | None = None,
                  src_order: int | None = None, stencil: int | None = None) -> Model:
     """Small heterogeneous test case with random (but stable) materials, random damping

@@ -22,6 +22,7 @@ import numpy as np
 
 from . import fields as F
 from . import inputs as I
+from . import runs
 from .solver import Batch, _check, load_library
 
 IN_PAD = 128          # inputs padded to one GEMM tile
@@ -349,9 +350,11 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> np.ndarray:
 
 
 def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: int = 1280, per_run: int = 64,
-                 seed: int = 7, max_offset: float = 12000.0, log=print) -> dict:
+                 seed: int = 7, max_offset: float = 12000.0, log=print) -> dict | None:
     """Runs the solver for train_runs + test_runs random source cells (depth 2-8 km, scaled to the
-    grid) and keeps, per source, `per_run` receivers with offsets in 1 km .. max_offset."""
+    grid) and keeps, per source, `per_run` receivers with offsets in 1 km .. max_offset.  Under
+    torch.distributed the sources are shared out over the ranks (elanfmt_gb300.runs) and only
+    rank 0 gets the dataset (None elsewhere)."""
     m = layered_iso(n=n, nt=nt)
     lpml = m.meta["lpml"]
     rec_xy = surface_receivers(n, lpml, 3)
@@ -368,9 +371,18 @@ def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: i
     for s in range(nrun):
         ok = np.nonzero((geo[s, :, 1] >= 1000) & (geo[s, :, 1] <= max_offset))[0]
         picks.append(np.sort(rng.choice(ok, size=min(per_run, len(ok)), replace=False)))
+    # independent solves: under torch.distributed every rank generates its share of the sources
+    # on its GPU and rank 0 gathers the traces (host side) and goes on alone
+    dist = _dist()
+    rank, world = (dist.get_rank(), dist.get_world_size()) if dist else (0, 1)
+    mine = list(runs.shard(nrun, rank, world))
     t0 = time.perf_counter()
-    traces, fdtd_s_per_src = generate(m, src, picks, rec_xy, log=log)
-    log(f"data: {nrun} sources in {time.perf_counter() - t0:.1f} s "
+    local, fdtd_s_per_src = generate(m, src[mine], [picks[s] for s in mine], rec_xy, log=log)
+    got = runs.gather(dict(zip(mine, local)), dist)
+    if got is None:
+        return None
+    traces = [got[s] for s in range(nrun)]
+    log(f"data: {nrun} sources on {world} GPU(s) in {time.perf_counter() - t0:.1f} s "
         f"({fdtd_s_per_src:.3f} device s per source, 6 RHS)")
     samples_src = np.concatenate([[s] * len(picks[s]) for s in range(nrun)]).astype(np.int64)
     samples_rec = np.concatenate(picks)
@@ -525,9 +537,20 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
     }
 
 
+def _dist():
+    try:
+        import torch.distributed as dist
+    except ImportError:
+        return None
+    return dist if dist.is_available() and dist.is_initialized() else None
+
+
 def study(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: int = 1280, per_run: int = 64,
-          steps: int = 6000, seed: int = 7, max_offset: float = 12000.0, log=print, **fit_kw) -> dict:
+          steps: int = 6000, seed: int = 7, max_offset: float = 12000.0, log=print, **fit_kw) -> dict | None:
+    """The whole study; None on ranks other than 0 of a multi-GPU run."""
     ds = make_dataset(train_runs, test_runs, n, nt, per_run, seed, max_offset, log)
+    if ds is None:
+        return None
     return fit_and_evaluate(ds, steps=steps, seed=seed, log=log, **fit_kw)
 
 
@@ -542,7 +565,18 @@ def main():
     ap.add_argument("--max-offset", type=float, default=12000.0)
     ap.add_argument("--out", default="")
     a = ap.parse_args()
+    import os
+
+    import torch
+
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1:  # torchrun: one rank per GPU, data generation sharded
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
     res = study(a.train_runs, a.test_runs, a.n, a.nt, per_run=a.per_run, steps=a.steps, max_offset=a.max_offset)
+    if res is None:
+        return
     print(json.dumps(res, indent=1))
     if a.out:
         with open(a.out, "w") as fh:

@@ -183,3 +183,21 @@ def test_oracle_isohet_agrees_with_mapped_orthorhombic_scheme():
     m.vdamp = F.VDAMP_16KM
     c = O.run(m, 30)
     assert not np.array_equal(a.traces, c.traces)
+
+
+def test_iso_het_layered_fields():
+    L = [{"top": 0, "vp": 3000.0, "vs": 1700.0, "rho": 2200.0}, {"top": 6, "vp": 5000.0, "vs": 2900.0, "rho": 2700.0}]
+    m = I.iso_het_layered(12, 10, 14, nt=5, dx=100.0, dt=0.005, layers=L, thick=3, margin_y=3)
+    mu1, mu2 = 2200.0 * 1700.0 ** 2, 2700.0 * 2900.0 ** 2
+    assert m.materials[F.M_C11].shape == (14, 10, 12)
+    assert m.materials[F.M_C11][0, 0, 0] == np.float32(2200.0 * 3000.0 ** 2)
+    assert m.materials[F.M_C12][10, 0, 0] == np.float32(2700.0 * 5000.0 ** 2 - 2 * mu2)
+    # edge moduli: harmonic means, zero on the border planes; interfaces mix the two layers
+    xz = m.materials[F.M_C55XZ]
+    assert xz.shape == (15, 10, 13) and xz[0].max() == 0 and xz[:, :, 0].max() == 0
+    assert xz[3, 4, 5] == np.float32(mu1) and xz[10, 4, 5] == np.float32(mu2)
+    assert np.isclose(xz[6, 4, 5], 4 / (2 / mu1 + 2 / mu2), rtol=1e-6)
+    bz = m.materials[F.M_BZ]
+    assert bz.shape == (15, 10, 12) and bz[0].max() == 0 and np.isclose(bz[6, 3, 3], (1 / 2200 + 1 / 2700) / 2)
+    w = m.damping_arrays[F.D_W3D]
+    assert w.shape == (14, 10, 12) and w[0, 5, 6] == 1.0 and w[-1, 5, 6] < 1.0
