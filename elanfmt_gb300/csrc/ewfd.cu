@@ -11,9 +11,12 @@
 #include "ewfd_fused.cuh"
 
 #include <cmath>
+#include <condition_variable>
 #include <cstdarg>
+#include <deque>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -193,7 +196,96 @@ struct ewf_handle {
     float last_ms = 0.f;
     int kchunk = 32;
     bool fdiv = false;  // div_spacing verified for (float) dx, dy, dz
+    struct Snapshots *snap = nullptr;  // queued snapshot writer (created on first use)
 };
+
+// ------------------------------------------------------------------------------------------
+// queued snapshots: device copy in stream order, D2H on a second stream, files by a thread
+// ------------------------------------------------------------------------------------------
+struct Snapshots {
+    struct Slot {
+        void *dev = nullptr;          // Vx | Vy | Vz in the reference layout
+        void *host = nullptr;         // pinned
+        cudaEvent_t ready = nullptr;  // device copy done (solver stream)
+        cudaEvent_t done = nullptr;   // D2H done (copy stream)
+        bool busy = false;
+        int isave = 0;
+    };
+    int device = 0;
+    size_t n[3] = {0, 0, 0};
+    size_t esz = 4;
+    std::string dir;
+    cudaStream_t copy = nullptr;
+    Slot slot[2];
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<int> queue;  // slots whose files are still to be written, oldest first
+    bool stop = false;
+    int error = EWF_OK;
+    std::string error_msg;
+    std::thread worker;
+
+    void run()
+    {
+        cudaSetDevice(device);
+        for (;;) {
+            int q;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || !queue.empty(); });
+                if (queue.empty()) return;
+                q = queue.front();
+            }
+            Slot &sl = slot[q];
+            int st = EWF_OK;
+            std::string msg;
+            if (cudaEventSynchronize(sl.done) != cudaSuccess) {
+                st = EWF_ERR_CUDA;
+                msg = "snapshot copy failed";
+                cudaGetLastError();
+            } else {
+                static const char *names[3] = {"Vx", "Vy", "Vz"};
+                const char *base = (const char *)sl.host;
+                for (int f = 0; f < 3 && st == EWF_OK; ++f) {
+                    char fn[64];
+                    snprintf(fn, sizeof(fn), "/%d_0_%s.res", sl.isave, names[f]);
+                    st = ewf_write_raw_file((dir + fn).c_str(), base, n[f] * esz);
+                    if (st) msg = ewf_last_error();
+                    base += n[f] * esz;
+                }
+            }
+            std::lock_guard<std::mutex> lk(mu);
+            if (st && error == EWF_OK) {
+                error = st;
+                error_msg = msg;
+            }
+            sl.busy = false;
+            queue.pop_front();
+            cv.notify_all();
+        }
+    }
+};
+
+static void snapshots_close(ewf_handle *h)
+{
+    Snapshots *S = h->snap;
+    if (!S) return;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->cv.notify_all();
+    if (S->worker.joinable()) S->worker.join();
+    for (auto &sl : S->slot) {
+        if (sl.dev) cudaFree(sl.dev);
+        if (sl.host) cudaFreeHost(sl.host);
+        if (sl.ready) cudaEventDestroy(sl.ready);
+        if (sl.done) cudaEventDestroy(sl.done);
+    }
+    if (S->copy) cudaStreamDestroy(S->copy);
+    delete S;
+    h->snap = nullptr;
+}
 
 static void *boxptr(const ewf_handle *h, void *alloc)
 {
@@ -317,6 +409,7 @@ extern "C" void ewf_destroy(ewf_handle *h)
     cudaGetDevice(&cur);
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    snapshots_close(h);  // finishes the queued snapshot files first
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     for (auto &x : h->f_alloc) cudaFree(x);
     for (auto &x : h->g_alloc) cudaFree(x);
@@ -559,6 +652,83 @@ extern "C" int ewf_get_field(ewf_handle *h, int32_t field, void *host, size_t n,
     CK(cudaMemcpyAsync(host, h->d_stage, n * dtype_bytes, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return EWF_OK;
+}
+
+extern "C" int ewf_write_snapshot_async(ewf_handle *h, int32_t isave)
+{
+    if (!h || isave < 0) return ewf_fail(EWF_ERR_ARG, "bad argument");
+    static const int ids[3] = {EWF_F_VX, EWF_F_VY, EWF_F_VZ};
+    if (!h->snap) {
+        Snapshots *S = new (std::nothrow) Snapshots();
+        if (!S) return ewf_fail(EWF_ERR_NOMEM, "host allocation");
+        h->snap = S;
+        S->device = h->device;
+        S->esz = h->esz;
+        S->dir = h->workdir;
+        size_t total = 0;
+        for (int f = 0; f < 3; ++f) total += (S->n[f] = ewf_field_size(h, ids[f]));
+        CK(cudaStreamCreateWithFlags(&S->copy, cudaStreamNonBlocking));
+        for (auto &sl : S->slot) {
+            CK(cudaMalloc(&sl.dev, total * S->esz));
+            CK(cudaMallocHost(&sl.host, total * S->esz));
+            CK(cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+        }
+        S->worker = std::thread([S] { S->run(); });
+    }
+    Snapshots *S = h->snap;
+    int q;
+    {
+        std::unique_lock<std::mutex> lk(S->mu);
+        S->cv.wait(lk, [&] { return !S->slot[0].busy || !S->slot[1].busy; });
+        q = S->slot[0].busy ? 1 : 0;
+        S->slot[q].busy = true;
+        S->slot[q].isave = isave;
+    }
+    Snapshots::Slot &sl = S->slot[q];
+    char *dst = (char *)sl.dev;
+    for (int f = 0; f < 3; ++f) {
+        int ex, ey, ez;
+        ewf_field_extent(h->p, ids[f], &ex, &ey, &ez);
+        bool is_box;
+        const void *src = field_dev(h, ids[f], &is_box);
+        const unsigned nb = pack_blocks(S->n[f]);
+        if (h->esz == 4)
+            k_unpack<float, float><<<nb, 256, 0, h->stream>>>((float *)dst, (const float *)src, ex, ey, ez, h->sx, h->sy);
+        else
+            k_unpack<double, double><<<nb, 256, 0, h->stream>>>((double *)dst, (const double *)src, ex, ey, ez, h->sx, h->sy);
+        dst += S->n[f] * S->esz;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(sl.ready, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(S->copy, sl.ready, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sl.host, sl.dev, (S->n[0] + S->n[1] + S->n[2]) * S->esz, cudaMemcpyDeviceToHost, S->copy);
+    if (e == cudaSuccess) e = cudaEventRecord(sl.done, S->copy);
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (e != cudaSuccess) {
+        sl.busy = false;
+        S->cv.notify_all();
+        return ewf_fail(EWF_ERR_CUDA, "snapshot: %s", cudaGetErrorString(e));
+    }
+    S->queue.push_back(q);
+    S->cv.notify_all();
+    return EWF_OK;
+}
+
+extern "C" int ewf_snapshot_wait(ewf_handle *h)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    Snapshots *S = h->snap;
+    if (!S) return EWF_OK;
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->cv.wait(lk, [&] { return S->queue.empty(); });
+    const int st = S->error;
+    if (st) {
+        ewf_fail(st, "%s", S->error_msg.c_str());
+        S->error = EWF_OK;
+    }
+    return st;
 }
 
 extern "C" int ewf_set_stf(ewf_handle *h, const double *stf, size_t n)

@@ -98,6 +98,8 @@ int save_field(ewf_handle *h, int isave, const char *name, int id)
 
 }  // namespace
 
+int ewf_write_raw_file(const char *path, const void *data, size_t bytes) { return write_raw(path, data, bytes); }
+
 extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
 {
     if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");

@@ -157,10 +157,11 @@ int main(int argc, char **argv)
         ewf_last_run_ms(h, &ms);
         total_ms += ms;
         done += chunk;
-        if (snap_every > 0 && done < p.nt) {
-            if ((st = ewf_write_snapshot(h, isave++))) { ewf_destroy(h); return fail(st, "snapshot"); }
+        if (snap_every > 0 && done < p.nt) {  /* written by the library while the next chunk runs */
+            if ((st = ewf_write_snapshot_async(h, isave++))) { ewf_destroy(h); return fail(st, "snapshot"); }
         }
     }
+    if ((st = ewf_snapshot_wait(h))) { ewf_destroy(h); return fail(st, "snapshot"); }
     if (!quiet) {
         const double cells = (double)p.nx * p.ny * p.nz * p.nt;
         printf("\n  time is %.3f s after %d iterations, %.2f Gcell-updates/s\n", total_ms * 1e-3, p.nt,

@@ -67,6 +67,8 @@ SIGNATURES = {
     "ewf_launches_per_step": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_write_legacy_outputs": (C.c_int, [C.c_void_p]),
     "ewf_write_snapshot": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_write_snapshot_async": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_snapshot_wait": (C.c_int, [C.c_void_p]),
     "ewf_pack_field_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int32,
                                          C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
@@ -151,7 +153,7 @@ class Solver:
     @classmethod
     def from_model(cls, m, precision: int = F.PREC_F32, kchunk: int = 0, graph_steps: int = 0,
                    check_finite: bool = True, damping: int | None = None, nout: int = 0,
-                   fused: bool | None = None) -> "Solver":
+                   fused: bool | None = None, workdir: str | None = None) -> "Solver":
         p = default_params()
         p.nx, p.ny, p.nz, p.nt = m.nx, m.ny, m.nz, m.nt
         p.model, p.precision = m.model, precision
@@ -163,6 +165,8 @@ class Solver:
         p.vdamp = getattr(m, "vdamp", 0.0)
         if fused is not None:
             p.fused = int(fused)
+        if workdir is not None:
+            p.workdir = os.fsencode(workdir)
         s = cls(p)
         try:
             s.set_model(m)
@@ -290,8 +294,16 @@ class Solver:
     def write_legacy_outputs(self) -> None:
         _check(self._lib.ewf_write_legacy_outputs(self._h), "ewf_write_legacy_outputs")
 
-    def write_snapshot(self, isave: int) -> None:
-        _check(self._lib.ewf_write_snapshot(self._h, isave), "ewf_write_snapshot")
+    def write_snapshot(self, isave: int, wait: bool = True) -> None:
+        """Vx, Vy, Vz to <isave>_0_V?.res in the work directory; wait=False queues the write and
+        returns at once (ewf_write_snapshot_async; see snapshot_wait)."""
+        if wait:
+            _check(self._lib.ewf_write_snapshot(self._h, isave), "ewf_write_snapshot")
+        else:
+            _check(self._lib.ewf_write_snapshot_async(self._h, isave), "ewf_write_snapshot_async")
+
+    def snapshot_wait(self) -> None:
+        _check(self._lib.ewf_snapshot_wait(self._h), "ewf_snapshot_wait")
 
     def checkpoint(self, path: str) -> None:
         _check(self._lib.ewf_checkpoint(self._h, os.fsencode(path)), "ewf_checkpoint")

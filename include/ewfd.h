@@ -184,6 +184,15 @@ int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
 int ewf_write_legacy_outputs(ewf_handle *h);
 /* Writes "<isave>_0_<name>.res" snapshots of Vx, Vy, Vz (the nsave stub of the 16 km scenario). */
 int ewf_write_snapshot(ewf_handle *h, int32_t isave);
+/* The same snapshot without stalling the time loop (the reference's nsave stub, 16kmst.cu:
+ * 478-484, made to work): Vx, Vy, Vz are copied on the device in the solver's stream order (later
+ * steps cannot overwrite them), brought to pinned host memory on a second stream while the next
+ * steps run, and written to <isave>_0_V?.res by a library thread.  Two snapshots may be in
+ * flight; a third call waits for the oldest to be written.  ewf_snapshot_wait blocks until every
+ * queued snapshot is on disk and returns the first write error (0 if none); ewf_destroy waits
+ * too. */
+int ewf_write_snapshot_async(ewf_handle *h, int32_t isave);
+int ewf_snapshot_wait(ewf_handle *h);
 
 /* Layout conversion that allocates nothing (no counterpart in the reference).
  *

@@ -239,3 +239,29 @@ def test_legacy_file_contract_through_ewfd(cuda_device, tmp_path):
         np.testing.assert_array_equal(s.seismograms(), ref.traces)
     finally:
         s.close()
+
+
+def test_async_snapshots_are_the_fields_at_their_step(cuda_device, tmp_path):
+    """Queued snapshots (device copy in stream order, D2H on a second stream, files by a library
+    thread) hold the fields of the step they were requested at, while later steps run; three
+    requests in a row exercise the wait for a free slot."""
+    m = I.random_small(F.MODEL_ORTHO, 30, 28, 22, nt=60, seed=4, damping=F.DAMP_W3D)
+    want = {}
+    with Solver.from_model(m, workdir=str(tmp_path)) as s:
+        for isave in (1, 2, 3):
+            s.run(12)
+            s.write_snapshot(isave, wait=False)
+            want[isave] = [s.field(q) for q in (F.F_VX, F.F_VY, F.F_VZ)]
+        s.write_snapshot(4, wait=False)
+        s.write_snapshot(5, wait=True)  # the synchronous form of the same step
+        s.run(12)
+        s.snapshot_wait()
+    for isave, fields in want.items():
+        for name, f in zip(("Vx", "Vy", "Vz"), fields):
+            got = np.fromfile(tmp_path / f"{isave}_0_{name}.res", np.float32).reshape(f.shape)
+            np.testing.assert_array_equal(got, f, err_msg=f"snapshot {isave} {name}")
+    for name in ("Vx", "Vy", "Vz"):
+        a = np.fromfile(tmp_path / f"4_0_{name}.res", np.float32)
+        b = np.fromfile(tmp_path / f"5_0_{name}.res", np.float32)
+        np.testing.assert_array_equal(a, b)
+    assert np.abs(want[3][2]).max() > 0
