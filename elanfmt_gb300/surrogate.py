@@ -554,8 +554,49 @@ def study(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: int = 12
     return fit_and_evaluate(ds, steps=steps, seed=seed, log=log, **fit_kw)
 
 
+def gemm_benchmark(shapes=((4096, 12800, 512), (4096, 512, 512), (256, 12800, 512), (12800, 512, 256),
+                            (8192, 8192, 8192)), reps: int = 20) -> list:
+    """TFLOP/s of ewf_mlp_gemm (C = A.B^T, bf16 in, fp32 out) against cuBLAS (torch.matmul, bf16 in,
+    fp32 accumulate) on the network's shapes (inference output layer, hidden layer, one training
+    batch, a weight gradient) and one large square problem; CUDA events, warm."""
+    import torch
+
+    lib = load_library()
+    out = []
+    g = torch.Generator(device="cpu").manual_seed(0)
+    for M, N, K in shapes:
+        A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+        B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+        C = torch.empty(M, N, device="cuda")
+        st = _stream()
+
+        def ours():
+            _check(lib.ewf_mlp_gemm(_p(A), _p(B), None, _p(C), None, None, M, N, K, 0, st), "ewf_mlp_gemm")
+
+        def cublas():
+            torch.matmul(A, B.T, out=Cb)
+
+        Cb = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
+        res = {"M": M, "N": N, "K": K}
+        for name, fn in (("ewf_mlp_gemm", ours), ("cublas_bf16", cublas)):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            res[name] = {"ms": round(ms, 4), "tflops": round(2.0 * M * N * K / (ms * 1e-3) / 1e12, 1)}
+        out.append(res)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--gemm-bench", action="store_true", help="only time ewf_mlp_gemm against cuBLAS")
     ap.add_argument("--train-runs", type=int, default=256)
     ap.add_argument("--test-runs", type=int, default=64)
     ap.add_argument("--n", type=int, default=192)
@@ -568,6 +609,14 @@ def main():
     import os
 
     import torch
+
+    if a.gemm_bench:
+        res = gemm_benchmark()
+        print(json.dumps(res, indent=1))
+        if a.out:
+            with open(a.out, "w") as fh:
+                json.dump(res, fh, indent=1)
+        return
 
     if int(os.environ.get("WORLD_SIZE", "1")) > 1:  # torchrun: one rank per GPU, data generation sharded
         import torch.distributed as dist
