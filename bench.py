@@ -5,7 +5,8 @@ Workload (default): the orthorhombic layered model, 320 x 320 x 256 cells, FP32,
 64 surface receivers x 3 components (seeded synthetic inputs, see elanfmt_gb300/inputs.py).
 One bench "step" is one full run of the workload through libewfd.so with the inputs resident in
 HBM; `value` = cell-updates per second over the K timed runs (CUDA events on the solver's stream,
-max over ranks).  The working set (~2.6 GB) is far larger than L2, so no flush is needed.
+max over ranks).  The working set (21 fields, ~2.7 GB in the padded layout) is far larger
+than L2, so no flush is needed.
 
 Also reported: `e2e` (the same runs through the C ABI from pinned host buffers, H2D of every
 input and D2H of the seismograms inside the timed region), `roofline` (algorithmic bytes of the

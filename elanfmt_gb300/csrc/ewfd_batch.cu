@@ -53,7 +53,7 @@ struct Prob {
 };
 
 struct Family {
-    int model, damping, rc;       // rc: compile-time RHS count of the kernels (1, 6) or 0
+    int model, damping;           // single-RHS problems of one (model, damping) share a launch
     std::vector<int> probs;       // problem indices
     BatchProb<float> *d_probs = nullptr;
     int *d_item0 = nullptr;
@@ -437,16 +437,16 @@ static int build_tables(ewf_batch *b)
     // problems with several RHS get their own launches (k_stress_mr / k_velocity_mr)
     b->fams.clear();
     b->mr.clear();
-    std::map<std::tuple<int, int, int>, int> fam_of;
+    std::map<std::pair<int, int>, int> fam_of;
     for (int i = 0; i < n; ++i) {
         if (b->probs[i].R > 1) {
             b->mr.push_back(i);
             continue;
         }
-        const auto key = std::make_tuple(b->probs[i].p.model, b->probs[i].p.damping, 1);
+        const auto key = std::make_pair(b->probs[i].p.model, b->probs[i].p.damping);
         if (!fam_of.count(key)) {
             fam_of[key] = (int)b->fams.size();
-            b->fams.push_back(Family{std::get<0>(key), std::get<1>(key), std::get<2>(key)});
+            b->fams.push_back(Family{key.first, key.second});
         }
         b->fams[fam_of[key]].probs.push_back(i);
     }

@@ -1,15 +1,18 @@
 // ewfd_batch.cuh -- batched time step: many problems (models of uneven size) x many right-hand
-// sides (sources) advanced by one launch per phase.
+// sides (sources) advanced together.
 //
 // A problem is one model (grid, materials, damping) with R right-hand sides (source sets); its R
-// state sets are separate boxes (rhs_stride elements apart) sharing the material arrays.  The
-// work list of a launch is (problem, z-chunk, y-tile, x-tile, RHS) with the RHS innermost, so
-// the R CTAs that update one tile for the R right-hand sides run back to back: the tile's
-// material planes come from HBM once and from L2 for the other R-1 (the 6 elementary moment
-// tensors of a moment-tensor inversion share one model).  Every item is the single-problem
-// column update (stress_column / velocity_column).  The launch is persistent: the grid is sized
-// to the GPU and each CTA strides over the work list, so problems of very different sizes share
-// one launch without a tail per problem.
+// state sets are separate boxes (rhs_stride elements apart) sharing the material arrays.
+// * Problems with several RHS (k_stress_mr / k_velocity_mr) get a launch of their own whose
+//   blockIdx.x runs over (x-tile, RHS) with the RHS fastest: the R CTAs that update one tile for
+//   the R right-hand sides are dispatched together, so the tile's material planes come from HBM
+//   once and from L2 for the other R-1 (the 6 elementary moment tensors of a moment-tensor
+//   inversion share one model).
+// * Single-RHS problems of one (model, damping) family share one persistent launch (k_bstress /
+//   k_bvelocity): the grid is sized to the GPU and each CTA strides over a work list of
+//   (problem, z-chunk, y-tile, x-tile) items, so models of very different sizes share one launch
+//   without a tail per problem.
+// Every item is the single-problem column update (stress_column / velocity_column).
 #pragma once
 #include "ewfd_fused.cuh"
 
