@@ -106,12 +106,21 @@ bool ewf_field_extent(const ewf_params &p, int id, int *ex, int *ey, int *ez)
     case EWF_D_WY: x = ny + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
     case EWF_D_WZ: x = nz + (p.damping == EWF_DAMP_PML1D ? 1 : 0); y = 1; z = 1; break;
     case EWF_D_W3D: break;
+    case EWF_D_PX: case EWF_D_PXY: case EWF_D_PXZ: case EWF_D_PY: case EWF_D_PYZ: case EWF_D_PZ: {
+        if (p.damping != EWF_DAMP_PERCOMP) return false;
+        static const int ax[6] = {1, 0, 0, 1, 1, 0}, ay[6] = {0, 1, 0, 1, 0, 1}, az[6] = {0, 0, 1, 0, 1, 1};
+        const int q = id - EWF_D_PX;
+        x = nx + ax[q]; y = ny + ay[q]; z = nz + az[q];
+        break;
+    }
     default: return false;
     }
     if ((id == EWF_M_C66XY || id == EWF_M_C55XZ || id == EWF_M_C44YZ || id == EWF_M_BX || id == EWF_M_BY ||
          id == EWF_M_BZ) && p.model == EWF_MODEL_ISO)
         return false;
-    if ((id == EWF_D_WX || id == EWF_D_WY || id == EWF_D_WZ) && p.damping == EWF_DAMP_W3D) return false;
+    if ((id == EWF_D_WX || id == EWF_D_WY || id == EWF_D_WZ) &&
+        (p.damping == EWF_DAMP_W3D || p.damping == EWF_DAMP_PERCOMP))
+        return false;
     if (id == EWF_D_W3D && p.damping != EWF_DAMP_W3D) return false;
     *ex = x; *ey = y; *ez = z;
     return true;
@@ -174,8 +183,9 @@ struct ewf_handle {
     void *m_alloc[12] = {};
     bool m_set[12] = {};
     void *w1[3] = {};
-    bool w_set[4] = {};
+    bool w_set[10] = {};       // WX WY WZ W3D, then PX PY PZ PXY PXZ PYZ
     void *w3_alloc = nullptr;
+    void *w6_alloc[6] = {};    // PERCOMP weight fields
     double *d_stf = nullptr;
     size_t nstf = 0;
     SrcEntry *d_src = nullptr;
@@ -306,6 +316,7 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     for (int q = 0; q < 12; ++q) a.m[q] = (const T *)boxptr(h, h->m_alloc[q]);
     for (int q = 0; q < 3; ++q) a.w1[q] = (const T *)h->w1[q];
     a.w3 = (const T *)boxptr(h, h->w3_alloc);
+    for (int q = 0; q < 6; ++q) a.w6[q] = (const T *)boxptr(h, h->w6_alloc[q]);
     a.sy = h->sy;
     a.sx = h->sx;
     a.R = 1;
@@ -327,6 +338,8 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     a.rdy = (T)1.0 / a.dy;
     a.rdz = (T)1.0 / a.dz;
     a.c66 = (T)h->p.c66;
+    a.c44 = (T)h->p.c44;
+    a.c55 = (T)h->p.c55;
     a.bx = (T)h->p.bx;
     a.by = (T)h->p.by;
     a.bz = (T)h->p.bz;
@@ -417,6 +430,7 @@ extern "C" void ewf_destroy(ewf_handle *h)
     for (auto &x : h->m_alloc) cudaFree(x);
     for (auto &x : h->w1) cudaFree(x);
     cudaFree(h->w3_alloc);
+    for (auto &x : h->w6_alloc) cudaFree(x);
     cudaFree(h->d_stf);
     cudaFree(h->d_src);
     cudaFree(h->d_rec_off);
@@ -440,8 +454,10 @@ static int validate_params(const ewf_params *p)
     if (p->nt < 1) return ewf_fail(EWF_ERR_ARG, "nt must be >= 1 (got %d)", p->nt);
     if (p->model < EWF_MODEL_ISO || p->model > EWF_MODEL_ISO_HET) return ewf_fail(EWF_ERR_ARG, "unknown model %d", p->model);
     if (p->precision < EWF_PREC_F32 || p->precision > EWF_PREC_F64) return ewf_fail(EWF_ERR_ARG, "unknown precision %d", p->precision);
-    if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D)
-        return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles (damping 0)");
+    if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D && p->damping != EWF_DAMP_PERCOMP)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles or per-component weights (damping 0 or 3)");
+    if (p->damping == EWF_DAMP_PERCOMP && (p->model != EWF_MODEL_ISO || p->fused))
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "per-component weights: isotropic model, two-kernel step");
     if (p->model != EWF_MODEL_ISO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the orthorhombic and 9 km schemes use a 3-D or separable weight field (damping 1 or 2)");
     if (p->model == EWF_MODEL_ISO_HET && p->fused)
@@ -521,6 +537,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
         if (slot_used(p->model, q)) CKH(alloc_box(h, &h->m_alloc[q]));
     if (p->damping == EWF_DAMP_W3D) {
         CKH(alloc_box(h, &h->w3_alloc));
+    } else if (p->damping == EWF_DAMP_PERCOMP) {
+        for (int q = 0; q < 6; ++q) CKH(alloc_box(h, &h->w6_alloc[q]));
     } else {
         const int n1[3] = {nx + 1, ny + 1, nz + 1};
         for (int q = 0; q < 3; ++q) {
@@ -574,6 +592,7 @@ static void *field_dev(ewf_handle *h, int id, bool *is_box)
     const int ms = material_slot(h->p.model, id);
     if (ms >= 0) return boxptr(h, h->m_alloc[ms]);
     if (id == EWF_D_W3D) return boxptr(h, h->w3_alloc);
+    if (id >= EWF_D_PX && id <= EWF_D_PYZ) return boxptr(h, h->w6_alloc[id - EWF_D_PX]);
     if (id >= EWF_D_WX && id <= EWF_D_WZ) {
         *is_box = false;
         return h->w1[id - EWF_D_WX];
@@ -622,7 +641,7 @@ extern "C" int ewf_set_field(ewf_handle *h, int32_t field, const void *host, siz
     CK(cudaStreamSynchronize(h->stream));
     const int ms = material_slot(h->p.model, field);
     if (ms >= 0) h->m_set[ms] = true;
-    if (field >= EWF_D_WX && field <= EWF_D_W3D) h->w_set[field - EWF_D_WX] = true;
+    if (field >= EWF_D_WX && field <= EWF_D_PYZ) h->w_set[field - EWF_D_WX] = true;
     return EWF_OK;
 }
 
@@ -935,6 +954,13 @@ static step_fn pick_step_t(const ewf_params &p)
 {
     const bool iso = p.model == EWF_MODEL_ISO;
     const bool w3 = p.damping == EWF_DAMP_W3D;
+    if (p.damping == EWF_DAMP_PERCOMP) {  // isotropic, two-kernel step only (validated)
+        switch (p.precision) {
+        case EWF_PREC_F32: return step_entry<float, MODEL_ISO, DAMP_PERCOMP, false>;
+        case EWF_PREC_F32_KAHAN: return step_entry<float, MODEL_ISO, DAMP_PERCOMP, true>;
+        default: return step_entry<double, MODEL_ISO, DAMP_PERCOMP, false>;
+        }
+    }
     if (p.model == EWF_MODEL_ISO_HET) {  // two-kernel step only (validated)
         switch (p.precision) {
         case EWF_PREC_F32:
@@ -966,6 +992,9 @@ static int inputs_ready(const ewf_handle *h)
         if (slot_used(h->p.model, q) && !h->m_set[q]) return ewf_fail(EWF_ERR_STATE, "material slot %d not set", q);
     if (h->p.damping == EWF_DAMP_W3D) {
         if (!h->w_set[3]) return ewf_fail(EWF_ERR_STATE, "3-D weights not set");
+    } else if (h->p.damping == EWF_DAMP_PERCOMP) {
+        for (int q = 4; q < 10; ++q)
+            if (!h->w_set[q]) return ewf_fail(EWF_ERR_STATE, "per-component weights %d not set", q - 4);
     } else {
         for (int q = 0; q < 3; ++q)
             if (!h->w_set[q]) return ewf_fail(EWF_ERR_STATE, "damping profile %d not set", q);

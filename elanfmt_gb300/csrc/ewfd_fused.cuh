@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(FX * FY, 2) k_step(const FusedArgs<T> fa)
 
     long long c = (long long)i + (long long)j * sx + (long long)ps * sy;
     T vx_m = T(0), vy_m = T(0), vz_k = T(0), wz_k = T(0);
-    StressIn<T, MODEL> nxt;
+    StressIn<T, MODEL, DAMP> nxt;
     if (in_grid) {
         vx_m = ld(a.f[0] + c - sy);
         vy_m = ld(a.f[1] + c - sy);
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(FX * FY, 2) k_step(const FusedArgs<T> fa)
         __syncthreads();  // buffer b was last read by V(p-2)
         if (compute) {
             if (in_grid) {
-                const StressIn<T, MODEL> q = nxt;
+                const StressIn<T, MODEL, DAMP> q = nxt;
                 if (p + 1 < nz && p + 1 <= k1) stress_load<T, MODEL, DAMP, 1>(a, c + sy, c + sy, p + 1, nxt);
                 const T Vxx = (q.vx_ip - q.vx) * rdx;
                 const T Vyy = (q.vy_jp - q.vy) * rdy;

@@ -24,7 +24,7 @@
 namespace ewf {
 
 enum { MODEL_ISO = 0, MODEL_ORTHO = 1, MODEL_ISOHET = 2 };
-enum { DAMP_PML1D = 0, DAMP_W3D = 1, DAMP_SEP = 2 };
+enum { DAMP_PML1D = 0, DAMP_W3D = 1, DAMP_SEP = 2, DAMP_PERCOMP = 3 };
 
 // Tile of the z-marching kernels: one thread per (i,j) column, a CTA covers TX x TY columns
 // and a chunk of planes.
@@ -38,6 +38,7 @@ struct StepArgs {
     const T *m[12];   // iso: c11 c12 | ortho: C11 C22 C33 C12 C13 C23 C66xy C55xz C44yz Bx By Bz
     const T *w1[3];   // iso: PML profiles (n+1 each) | separable: per-axis factors (n each)
     const T *w3;      // 3-D damping field (box layout)
+    const T *w6[6];   // per-component weights of Vx/sxx, Vy/syy, Vz/szz, sxy, sxz, syz (box layout)
     long long sy;     // plane pitch of materials / damping, elements
     int sx;           // row pitch of materials / damping, elements
     int R;            // right-hand sides interleaved along x in the state arrays (1: one source)
@@ -48,6 +49,7 @@ struct StepArgs {
     int kchunk;       // planes per CTA
     T dt, rdt, dx, dy, dz, rdx, rdy, rdz;
     T c66, bx, by, bz;  // isotropic scalars (OK4:405-407)
+    T c44, c55;         // per-component-weight scheme: shear moduli of yz and xz
     T third;            // (T)1/(T)3 of BC1
     int fdiv;           // 1: div_spacing may take the reciprocal path for dx, dy, dz (verified)
     T vdamp;            // linear velocity damping (16 km scheme), 0 = off
@@ -93,7 +95,7 @@ __device__ __forceinline__ double div_spacing(double x, double d, double, bool) 
 // loads are issued before the current plane is computed, so ~25 independent loads per thread
 // are always in flight; conditional updates become predicated stores.
 // ---------------------------------------------------------------------------------------------
-template <typename T, int MODEL>
+template <typename T, int MODEL, int DAMP>
 struct StressIn {
     T vx, vx_ip, vx_jm;        // Vx(i,j,k), Vx(i+1), Vx(j-1)
     T vy, vy_jp, vy_im;        // Vy(i,j,k), Vy(j+1), Vy(i-1)
@@ -101,11 +103,13 @@ struct StressIn {
     T s[6];                    // sxx syy szz sxy sxz syz at (i,j,k)
     T c[MODEL == MODEL_ISO ? 2 : (MODEL == MODEL_ISOHET ? 5 : 9)];
     T w;                       // iso: wz[k+1]; ortho, iso-het: W or pz[k]
+    T pw[DAMP == DAMP_PERCOMP ? 6 : 1];  // per-component weights at the cell
 };
 
 // c: state index (x stride R), cm: material index of the same cell
 template <typename T, int MODEL, int DAMP, int RC>
-__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k, StressIn<T, MODEL> &q)
+__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k,
+                                            StressIn<T, MODEL, DAMP> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
@@ -124,7 +128,12 @@ __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, l
     if (MODEL == MODEL_ISO) {
         q.c[0] = ld(a.m[0] + cm);
         q.c[1] = ld(a.m[1] + cm);
-        q.w = ld(a.w1[2] + k + 1);
+        if (DAMP == DAMP_PERCOMP) {
+#pragma unroll
+            for (int f = 0; f < 6; ++f) q.pw[f] = ld(a.w6[f] + cm);
+        } else {
+            q.w = ld(a.w1[2] + k + 1);
+        }
     } else if (MODEL == MODEL_ISOHET) {
         q.c[0] = ld(a.m[0] + cm);  // c11u_het
         q.c[1] = ld(a.m[3] + cm);  // c12u_het
@@ -172,19 +181,32 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
     T vz_k = ld(a.f[2] + c);        // Vz(k)
     T wz_k = T(0);
     if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + k0);
-    StressIn<T, MODEL> nxt;
+    StressIn<T, MODEL, DAMP> nxt;
     stress_load<T, MODEL, DAMP, RC>(a, c, SEP ? cm : c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sys) {
         if (SEP && k > k0) cm += sy;
-        const StressIn<T, MODEL> q = nxt;
+        const StressIn<T, MODEL, DAMP> q = nxt;
         if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
         const T Vxx = (q.vx_ip - q.vx) * rdx;
         const T Vyy = (q.vy_jp - q.vy) * rdy;
         const T Vzz = (q.vz_p - vz_k) * rdz;
         T sxx, syy, szz, sxy, sxz, syz;
         bool w_xy = true, w_xz = true, w_yz = true;
-        if (MODEL == MODEL_ISO) {
+        if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
+            const T c11 = q.c[0], c12 = q.c[1];
+            // DC_Earthquake FastWaveED_GPU3D_v1.cu:313-315: each component's own 3-D weight
+            sxx = q.pw[0] * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
+            syy = q.pw[1] * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
+            szz = q.pw[2] * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
+            // :318-320, the shear moduli c66 (xy), c55 (xz), c44 (yz); guarded like ANISO
+            sxy = q.pw[3] * (q.s[3] + a.c66 * dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
+            sxz = q.pw[4] * (q.s[4] + a.c55 * dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
+            syz = q.pw[5] * (q.s[5] + a.c44 * dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
+            w_xy = (i > 0 && j > 0);
+            w_xz = (i > 0 && k > 0);
+            w_yz = (j > 0 && k > 0);
+        } else if (MODEL == MODEL_ISO) {
             const T c11 = q.c[0], c12 = q.c[1];
             // OK4:307-309
             sxx = wavx * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
@@ -292,7 +314,7 @@ __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, 
 // KAHAN: V = a*V + inc with the rounding error carried in comp[] (compensated summation).
 // Same structure as k_stress: hoisted, prefetched loads; predicated stores.
 // ---------------------------------------------------------------------------------------------
-template <typename T, int MODEL, bool KAHAN>
+template <typename T, int MODEL, int DAMP, bool KAHAN>
 struct VelIn {
     T sxx, sxx_im, syy, syy_jm, szz;
     T sxy, sxy_jp, sxy_ip;
@@ -300,11 +322,13 @@ struct VelIn {
     T v[3];
     T b[MODEL == MODEL_ISO ? 1 : 3];
     T w;                              // iso: wz[k-1]; ortho: W or pz[k]
+    T pw[DAMP == DAMP_PERCOMP ? 3 : 1];  // per-component weights of Vx, Vy, Vz
     T cp[KAHAN ? 3 : 1];
 };
 
 template <typename T, int MODEL, int DAMP, bool KAHAN, int RC>
-__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k, VelIn<T, MODEL, KAHAN> &q)
+__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k,
+                                         VelIn<T, MODEL, DAMP, KAHAN> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
@@ -323,7 +347,10 @@ __device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long
     q.syz_jp = ld(a.f[8] + c + sx);
 #pragma unroll
     for (int f = 0; f < 3; ++f) q.v[f] = a.f[f][c];
-    if (MODEL == MODEL_ISO) {
+    if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) q.pw[f] = ld(a.w6[f] + cm);
+    } else if (MODEL == MODEL_ISO) {
         q.w = ld(a.w1[2] + k - 1);
     } else {
 #pragma unroll
@@ -385,18 +412,22 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
     T szz_m = ld(a.f[5] + c - sys);
     T sxz_k = ld(a.f[7] + c);
     T syz_k = ld(a.f[8] + c);
-    VelIn<T, MODEL, KAHAN> nxt;
+    VelIn<T, MODEL, DAMP, KAHAN> nxt;
     vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c, SEP ? cm : c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sys) {
         if (SEP && k > k0) cm += sy;
-        VelIn<T, MODEL, KAHAN> q = nxt;
+        VelIn<T, MODEL, DAMP, KAHAN> q = nxt;
         if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
         const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
         const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
         const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;
         T ax, ay, az, bx, by, bz;
-        if (MODEL == MODEL_ISO) {
+        if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
+            // DC_Earthquake FastWaveED_GPU3D_v1.cu:344-360: each component's own 3-D weight
+            ax = q.pw[0]; ay = q.pw[1]; az = q.pw[2];
+            bx = a.bx; by = a.by; bz = a.bz;
+        } else if (MODEL == MODEL_ISO) {
             ax = wxm; ay = wym; az = q.w;
             bx = a.bx; by = a.by; bz = a.bz;
         } else {

@@ -121,7 +121,8 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
     // from these files (ewf_legacy_params)
     if (std::fabs(p.dx - dx) > 0 || std::fabs(p.dy - dy) > 0 || std::fabs(p.dz - dz) > 0 || std::fabs(p.dt - dt) > 0 ||
         (p.model == EWF_MODEL_ISO && (p.c66 != (double)pa2[7] || p.bx != (double)pa3[0] || p.by != (double)pa3[1] ||
-                                      p.bz != (double)pa3[2])))
+                                      p.bz != (double)pa3[2])) ||
+        (p.damping == EWF_DAMP_PERCOMP && (p.c44 != (double)pa2[5] || p.c55 != (double)pa2[6])))
         return ewf_fail(EWF_ERR_STATE,
                         "handle parameters differ from pa1/pa2/pa3.dat: create the handle with ewf_legacy_params() first");
 
@@ -130,9 +131,21 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
         std::vector<float> c11;
         if ((st = load_field(h, dir, "c11u_het.dat", EWF_M_C11, &c11))) return st;
         if ((st = load_field(h, dir, "c12u_het.dat", EWF_M_C12))) return st;
-        if ((st = load_field(h, dir, "weights_x.dat", EWF_D_WX))) return st;
-        if ((st = load_field(h, dir, "weights_y.dat", EWF_D_WY))) return st;
-        if ((st = load_field(h, dir, "weights_z.dat", EWF_D_WZ))) return st;
+        if (p.damping == EWF_DAMP_PERCOMP) {
+            // DC_Earthquake: 3-D weights per component, in the extents its driver writes them
+            // (vizme_FastWaveED_GPU3D.m:319-324; the solver itself reads only nx*ny*nz values of
+            // the shear ones, FastWaveED_GPU3D_v1.cu:406-410, then indexes them with edge pitches)
+            static const struct { const char *file; int id; } wf[] = {
+                {"weights_x.dat", EWF_D_PX},   {"weights_y.dat", EWF_D_PY},   {"weights_z.dat", EWF_D_PZ},
+                {"weights_xy.dat", EWF_D_PXY}, {"weights_xz.dat", EWF_D_PXZ}, {"weights_yz.dat", EWF_D_PYZ},
+            };
+            for (const auto &f : wf)
+                if ((st = load_field(h, dir, f.file, f.id))) return st;
+        } else {
+            if ((st = load_field(h, dir, "weights_x.dat", EWF_D_WX))) return st;
+            if ((st = load_field(h, dir, "weights_y.dat", EWF_D_WY))) return st;
+            if ((st = load_field(h, dir, "weights_z.dat", EWF_D_WZ))) return st;
+        }
         double cmax = 0;
         for (float v : c11) cmax = std::max(cmax, (double)v);
         const double bmax = std::max({(double)pa3[0], (double)pa3[1], (double)pa3[2]});
@@ -189,7 +202,15 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
     const int ysrc = (int)std::round((Ly - Ly / 2.0) / dy);
     double mt[6];
     int xsrc, zsrc, stencil;
-    if (p.model == EWF_MODEL_ISO) {
+    if (p.model == EWF_MODEL_ISO && p.damping == EWF_DAMP_PERCOMP) {
+        // DC_Earthquake's source kernel adds 1.0 Src to sxz and 0.8 Src to syz only, at the
+        // ANISO stencil cells (FastWaveED_GPU3D_v1.cu:228-246, 436-438)
+        const double c[6] = {0.0, 0.0, 0.0, 0.0, 1.0, (double)0.8f};
+        for (int q = 0; q < 6; ++q) mt[q] = c[q];
+        xsrc = 234;
+        zsrc = 100;
+        stencil = 1;
+    } else if (p.model == EWF_MODEL_ISO) {
         std::vector<float> mts;
         if ((st = read_f32(join(dir, "MTS.dat"), 6, false, mts))) return st;
         for (int q = 0; q < 6; ++q) mt[q] = mts[q];
@@ -215,7 +236,10 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
 
     // the four legacy traces Rec, Rec_x, Rec_y, Rec_y2 (OK4:383-386 / ANISO:263-266)
     int32_t rec[16];
-    if (p.model == EWF_MODEL_ISO) {
+    if (p.model == EWF_MODEL_ISO && p.damping == EWF_DAMP_PERCOMP) {  // FastWaveED_GPU3D_v1.cu:278-281
+        const int32_t r[16] = {504, 129, 1, EWF_F_VZ, 504, 129, 1, EWF_F_VX, 504, 132, 1, EWF_F_VY, 504, 131, 1, EWF_F_VY};
+        memcpy(rec, r, sizeof(r));
+    } else if (p.model == EWF_MODEL_ISO) {
         const int32_t r[16] = {504, 385, 1, EWF_F_VZ, 504, 385, 1, EWF_F_VX, 504, 388, 1, EWF_F_VY, 504, 387, 1, EWF_F_VY};
         memcpy(rec, r, sizeof(r));
     } else {
@@ -285,6 +309,8 @@ extern "C" int ewf_legacy_params(ewf_params *p)
     if ((st = read_f32(join(dir, "pa3.dat"), 3, false, pa3))) return st;
     p->dx = pa1[0]; p->dy = pa1[1]; p->dz = pa1[2]; p->dt = pa1[3];
     p->c66 = pa2[7];
+    p->c44 = pa2[5];
+    p->c55 = pa2[6];
     p->bx = pa3[0]; p->by = pa3[1]; p->bz = pa3[2];
     if (p->nt <= 0) {
         const size_t n = file_floats(join(dir, "Src.dat"));

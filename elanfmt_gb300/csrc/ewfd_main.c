@@ -7,7 +7,7 @@
  * (nx = 64*NBX - OVERX, OK4:29-41) or directly as --nx/--ny/--nz; everything else is read from
  * the same files and written to the same 0_infos.inf / 0_0_*.res outputs (OK4:521-532).
  *
- *   ewfd --nbx 12 --nby 12 --nbz 7 [--overx 0 ...] [--model iso|ortho|isohet] [--nt N] [--vdamp C]
+ *   ewfd --nbx 12 --nby 12 --nbz 7 [--overx 0 ...] [--model iso|ortho|isohet|dcq] [--nt N] [--vdamp C]
  *        [--precision f32|kahan|f64] [--src i,j,k] [--stencil ok4|aniso] [--mts FILE]
  *        [--receivers FILE] [--snap-every N] [--workdir DIR] [--quiet] [--no-checks]
  *
@@ -65,7 +65,7 @@ int main(int argc, char **argv)
     ewf_params p;
     ewf_params_default(&p);
     int nbx = 0, nby = 0, nbz = 0, overx = 0, overy = 0, overz = 0;
-    int src[3] = {-1, -1, -1}, stencil = -1, snap_every = 0, quiet = 0;
+    int src[3] = {-1, -1, -1}, stencil = -1, snap_every = 0, quiet = 0, percomp = 0;
     const char *mts_file = NULL, *rec_file = NULL;
     p.workdir = ".";
     p.nout = 200;
@@ -81,8 +81,9 @@ int main(int argc, char **argv)
         if (!strcmp(k, "--model") && v) {
             if (!strcmp(v, "ortho")) p.model = EWF_MODEL_ORTHO;
             else if (!strcmp(v, "isohet")) p.model = EWF_MODEL_ISO_HET; /* the 9 km station scheme */
+            else if (!strcmp(v, "dcq")) { p.model = EWF_MODEL_ISO; percomp = 1; } /* DC_Earthquake */
             else if (!strcmp(v, "iso")) p.model = EWF_MODEL_ISO;
-            else return fail(EWF_ERR_ARG, "--model iso|ortho|isohet");
+            else return fail(EWF_ERR_ARG, "--model iso|ortho|isohet|dcq");
             ++a;
             continue;
         }
@@ -106,8 +107,8 @@ int main(int argc, char **argv)
     if (p.ny <= 0 && nby > 0) p.ny = 64 * nby - overy;
     if (p.nz <= 0 && nbz > 0) p.nz = 64 * nbz - overz;
     p.over_y = overy;
-    p.damping = p.model == EWF_MODEL_ISO ? EWF_DAMP_PML1D : EWF_DAMP_W3D;
-    p.src_order = p.model == EWF_MODEL_ISO ? EWF_SRC_BEFORE_BC1 : EWF_SRC_AFTER_BC1;
+    p.damping = percomp ? EWF_DAMP_PERCOMP : p.model == EWF_MODEL_ISO ? EWF_DAMP_PML1D : EWF_DAMP_W3D;
+    p.src_order = (p.model == EWF_MODEL_ISO && !percomp) ? EWF_SRC_BEFORE_BC1 : EWF_SRC_AFTER_BC1;
     if (p.nx <= 0 || p.ny <= 0 || p.nz <= 0) {
         fprintf(stderr, "ewfd: give the grid as --nbx/--nby/--nbz [--overx..] or --nx/--ny/--nz\n");
         return 1;
@@ -136,7 +137,7 @@ int main(int argc, char **argv)
             ewf_destroy(h);
             return 1;
         }
-        const int sten = stencil >= 0 ? stencil : (p.model == EWF_MODEL_ISO ? 0 : 1);
+        const int sten = stencil >= 0 ? stencil : (p.model == EWF_MODEL_ISO && !percomp ? 0 : 1);
         if ((st = ewf_set_moment_tensor(h, mt, src[0], src[1], src[2], sten))) { ewf_destroy(h); return fail(st, "source"); }
     }
     if (rec_file) {

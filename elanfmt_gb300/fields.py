@@ -11,7 +11,7 @@ import numpy as np
 # ewf_model / ewf_precision / ewf_damping / ewf_src_order
 MODEL_ISO, MODEL_ORTHO, MODEL_ISO_HET = 0, 1, 2
 PREC_F32, PREC_F32_KAHAN, PREC_F64 = 0, 1, 2
-DAMP_PML1D, DAMP_W3D, DAMP_SEPARABLE = 0, 1, 2
+DAMP_PML1D, DAMP_W3D, DAMP_SEPARABLE, DAMP_PERCOMP = 0, 1, 2, 3
 SRC_BEFORE_BC1, SRC_AFTER_BC1 = 0, 1
 
 # state fields
@@ -30,6 +30,9 @@ ISOHET_MATERIALS = (M_C11, M_C12, M_C66XY, M_C55XZ, M_C44YZ, M_BX, M_BY, M_BZ)
 VDAMP_16KM = float(np.float32(np.float32(2.2) * np.float32(4.6729e-04)))
 # damping
 D_WX, D_WY, D_WZ, D_W3D = 32, 33, 34, 35
+# per-component weights (DC_Earthquake solver): Vx/sxx, Vy/syy, Vz/szz, sxy, sxz, syz layouts
+D_PX, D_PY, D_PZ, D_PXY, D_PXZ, D_PYZ = 36, 37, 38, 39, 40, 41
+PERCOMP_WEIGHTS = (D_PX, D_PY, D_PZ, D_PXY, D_PXZ, D_PYZ)
 
 # status codes
 STATUS = {
@@ -50,6 +53,8 @@ LEGACY_FILES = {
     M_BZ: (None, "vrho_z_11_hc.dat", "vrho_z_11_hc.dat"),
     D_WX: ("weights_x.dat", None, None), D_WY: ("weights_y.dat", None, None), D_WZ: ("weights_z.dat", None, None),
     D_W3D: (None, "weights.dat", "weights.dat"),
+    D_PX: ("weights_x.dat", None, None), D_PY: ("weights_y.dat", None, None), D_PZ: ("weights_z.dat", None, None),
+    D_PXY: ("weights_xy.dat", None, None), D_PXZ: ("weights_xz.dat", None, None), D_PYZ: ("weights_yz.dat", None, None),
 }
 
 
@@ -71,6 +76,8 @@ def extent(fid: int, nx: int, ny: int, nz: int, damping: int = DAMP_PML1D) -> tu
     elif fid in (D_WX, D_WY, D_WZ):
         n = (nx, ny, nz)[fid - D_WX] + (1 if damping == DAMP_PML1D else 0)
         return n, 1, 1
+    elif fid in PERCOMP_WEIGHTS:  # the layout of the component each weights
+        return extent((F_VX, F_VY, F_VZ, F_SXY, F_SXZ, F_SYZ)[fid - D_PX], nx, ny, nz)
     return x, y, z
 
 
@@ -127,6 +134,9 @@ ANISO_LEGACY_MT = tuple(float(np.float32(v)) for v in (-0.6282, 0.9437, 0.2439, 
 # the 16 km station solver hard-codes another tensor in the same kernel and stencil
 # (FastWaveED_GPU3D_v1_16kmst.cu:228-252)
 ISO16KM_LEGACY_MT = tuple(float(np.float32(v)) for v in (-0.7448, 1.0603, 0.2439, -0.0387, -0.1953, -0.3017))
+# the DC_Earthquake solver's source kernel injects only xz (1.0) and yz (0.8) at the ANISO stencil
+# cells (src/FastWaveED_GPU3D_v1_DC_Earthquake/FastWaveED_GPU3D_v1.cu:228-246)
+DCQ_LEGACY_MT = (0.0, 0.0, 0.0, 0.0, 1.0, float(np.float32(0.8)))
 # the four legacy traces Rec, Rec_x, Rec_y, Rec_y2 (FastWaveED_GPU3D_v1.cu:383-386; ANISO:263-266)
 OK4_LEGACY_RECEIVERS = ((504, 385, 1, F_VZ), (504, 385, 1, F_VX), (504, 388, 1, F_VY), (504, 387, 1, F_VY))
 ANISO_LEGACY_RECEIVERS = ((631, 257, 1, F_VZ), (631, 257, 1, F_VX), (631, 257, 1, F_VY), (631, 257, 1, F_VY))

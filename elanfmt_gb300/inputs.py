@@ -279,6 +279,8 @@ class Model:
     by: float = 0.0
     bz: float = 0.0
     vdamp: float = 0.0    # linear velocity damping of the 16 km scheme (0 = off)
+    c44: float = 0.0      # per-component-weight scheme: shear moduli of yz and xz (c66: xy)
+    c55: float = 0.0
     materials: dict = field(default_factory=dict)   # field id -> float32 array
     damping_arrays: dict = field(default_factory=dict)  # EWF_D_* -> float32 array
     sources: np.ndarray | None = None   # (n, 4) int32: comp, i, j, k
@@ -459,7 +461,28 @@ def random_small(model: int, nx: int, ny: int, nz: int, nt: int, seed: int, damp
     vsf = vpf / rng.uniform(1.6, 2.0, size=(nz, ny, nx))
     c33 = rho * vpf**2
     mu = rho * vsf**2
-    if model == F.MODEL_ISO:
+    if model == F.MODEL_ISO and damping == F.DAMP_PERCOMP:
+        # the DC_Earthquake solver: c11/c12 fields, three shear scalars, a weight field per
+        # component (random near the faces), the ANISO loop order
+        m.damping = F.DAMP_PERCOMP
+        m.src_order = F.SRC_AFTER_BC1 if src_order is None else src_order
+        m.materials[F.M_C11] = c33.astype(np.float32)
+        m.materials[F.M_C12] = (c33 - 2 * mu).astype(np.float32)
+        m.c66 = float(np.float32(np.median(mu)))
+        m.c55 = float(np.float32(np.median(mu) * 1.03))
+        m.c44 = float(np.float32(np.median(mu) * 0.97))
+        m.bx, m.by, m.bz = (float(np.float32(1 / 2500.0)), float(np.float32(1 / 2600.0)), float(np.float32(1 / 2400.0)))
+        for fid in F.PERCOMP_WEIGHTS:
+            shp = F.shape(fid, nx, ny, nz)
+            w = np.ones(shp, np.float32)
+            for ax in range(3):
+                sl = [slice(None)] * 3
+                sl[ax] = slice(0, 3)
+                w[tuple(sl)] *= rng.uniform(0.9, 1.0, size=w[tuple(sl)].shape).astype(np.float32)
+                sl[ax] = slice(shp[ax] - 3, shp[ax])
+                w[tuple(sl)] *= rng.uniform(0.9, 1.0, size=w[tuple(sl)].shape).astype(np.float32)
+            m.damping_arrays[fid] = w
+    elif model == F.MODEL_ISO:
         m.damping = F.DAMP_PML1D
         m.src_order = F.SRC_BEFORE_BC1 if src_order is None else src_order
         m.materials[F.M_C11] = c33.astype(np.float32)
@@ -519,7 +542,7 @@ def random_small(model: int, nx: int, ny: int, nz: int, nt: int, seed: int, damp
             m.damping_arrays[F.D_WX], m.damping_arrays[F.D_WY], m.damping_arrays[F.D_WZ] = px, py, pz
         else:
             m.damping_arrays[F.D_W3D] = separable_weights(px, py, pz) * rng.uniform(0.999, 1.0, size=(nz, ny, nx)).astype(np.float32)
-    st = (0 if model == F.MODEL_ISO else 1) if stencil is None else stencil
+    st = (0 if model == F.MODEL_ISO and m.damping != F.DAMP_PERCOMP else 1) if stencil is None else stencil
     mt = rng.normal(size=6)
     xs, ys, zs = nx // 2 - 2, ny // 2 - 1, nz // 2 - 1
     m.set_moment_tensor(mt, xs, ys, zs, stencil=st)

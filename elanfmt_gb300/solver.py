@@ -33,7 +33,8 @@ class Params(C.Structure):
         ("over_y", C.c_int32), ("nout", C.c_int32), ("kchunk", C.c_int32), ("graph_steps", C.c_int32),
         ("check_finite", C.c_int32), ("fused", C.c_int32),
         ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
-        ("c66", C.c_double), ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
+        ("c66", C.c_double), ("c44", C.c_double), ("c55", C.c_double),
+        ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
         ("vdamp", C.c_double),
         ("workdir", C.c_char_p),
     ]
@@ -162,6 +163,7 @@ class Solver:
         p.kchunk, p.graph_steps, p.check_finite = kchunk, graph_steps, int(check_finite)
         p.dx, p.dy, p.dz, p.dt = m.dx, m.dy, m.dz, m.dt
         p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
+        p.c44, p.c55 = getattr(m, "c44", 0.0), getattr(m, "c55", 0.0)
         p.vdamp = getattr(m, "vdamp", 0.0)
         if fused is not None:
             p.fused = int(fused)
@@ -347,6 +349,7 @@ def params_for(m, precision: int = F.PREC_F32, kchunk: int = 0) -> Params:
     p.kchunk = kchunk
     p.dx, p.dy, p.dz, p.dt = m.dx, m.dy, m.dz, m.dt
     p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
+    p.c44, p.c55 = getattr(m, "c44", 0.0), getattr(m, "c55", 0.0)
     p.vdamp = getattr(m, "vdamp", 0.0)
     return p
 

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define EWF_ABI_VERSION 2
+#define EWF_ABI_VERSION 3
 
 typedef enum ewf_status {
     EWF_OK = 0,
@@ -60,7 +60,12 @@ typedef enum ewf_precision {
 typedef enum ewf_damping {
     EWF_DAMP_PML1D = 0,    /* 1-D profiles weights_x/y/z (n+1 each), OK4 usage (OK4:307-329, 361-375) */
     EWF_DAMP_W3D = 1,      /* 3-D weights field (nx,ny,nz), ANISO usage (ANISO:312-386) */
-    EWF_DAMP_SEPARABLE = 2 /* ANISO usage with W[i,j,k] = (px[i]*py[j])*pz[k] formed on the fly */
+    EWF_DAMP_SEPARABLE = 2, /* ANISO usage with W[i,j,k] = (px[i]*py[j])*pz[k] formed on the fly */
+    EWF_DAMP_PERCOMP = 3    /* isotropic model only: one 3-D weight field per stress component, the
+                             * normal-stress ones also weighting the velocities, w*(sigma + ...) and
+                             * w*(V/dt + b*div)*dt, shear moduli c66 (xy), c55 (xz), c44 (yz): the
+                             * DC_Earthquake solver (src/FastWaveED_GPU3D_v1_DC_Earthquake/
+                             * FastWaveED_GPU3D_v1.cu:298-320, 344-360), ANISO's loop order */
 } ewf_damping;
 
 typedef enum ewf_src_order {
@@ -85,7 +90,10 @@ typedef enum ewf_field {
     EWF_M_BZ = 27,    /* (nx,ny,nz+1) vrho_z_11_hc.dat */
     /* damping */
     EWF_D_WX = 32, EWF_D_WY = 33, EWF_D_WZ = 34, /* PML1D: n+1 each (weights_x/y/z.dat); SEPARABLE: n each */
-    EWF_D_W3D = 35                               /* (nx,ny,nz) weights.dat */
+    EWF_D_W3D = 35,                              /* (nx,ny,nz) weights.dat */
+    /* PERCOMP weights in their component's layout: weights_x/y/z.dat (Vx, Vy, Vz extents),
+     * weights_xy/xz/yz.dat (sxy, sxz, syz extents, as the DC_Earthquake driver writes them) */
+    EWF_D_PX = 36, EWF_D_PY = 37, EWF_D_PZ = 38, EWF_D_PXY = 39, EWF_D_PXZ = 40, EWF_D_PYZ = 41
 } ewf_field;
 
 typedef struct ewf_params {
@@ -102,7 +110,8 @@ typedef struct ewf_params {
     int32_t check_finite; /* 1: ewf_run checks the receiver traces for NaN/Inf */
     int32_t fused;        /* 0 (default): stress and velocity kernels; 1: one-pass step kernel (double-buffered state) */
     double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
-    double c66;            /* isotropic shear modulus pa2[7] (OK4:405) */
+    double c66;            /* isotropic shear modulus pa2[7] (OK4:405); PERCOMP: the xy one */
+    double c44, c55;       /* PERCOMP shear moduli of yz and xz, pa2[5], pa2[6] */
     double bx, by, bz;     /* isotropic 1/rho pa3[0..2] (OK4:407) */
     double vdamp;          /* linear velocity damping: V_new = update - vdamp * V_old (16 km station
                             * scheme, FastWaveED_GPU3D_v1_16kmst.cu:337-349, vdamp = 2.2 * 4.6729e-04

@@ -5,7 +5,8 @@
 * ``_ref/*.cubin``     -- the reference solvers' device code compiled from the reference sources
   where they lie (only where the reference tree is present; the cubins then travel with the
   repository copy).  The isotropic (OK4), orthorhombic (ANISO), 9 km (isotropic with edge shear
-  moduli) and 16 km (the 9 km scheme with linear velocity damping) solvers, each with the
+  moduli), 16 km (the 9 km scheme with linear velocity damping) and DC_Earthquake (isotropic
+  with per-component weights) solvers, each with the
   reference's own flags (``-O3``, FMA contraction on: "stock") and with ``--fmad=false``
   ("exact", every operation rounded on its own, which the oracle matches bit for bit).
 
@@ -30,6 +31,7 @@ REF_SOURCES = {
     "aniso": "src/FastWaveED_GPU3D_v1_9km_station_ANISO/FastWaveED_GPU3D_v1_9kmst_ANISO.cu",
     "iso9km": "src/FastWaveED_GPU3D_v1_9km_station/FastWaveED_GPU3D_v1_9kmst.cu",
     "iso16km": "src/FastWaveED_GPU3D_v1_16km_station/FastWaveED_GPU3D_v1_16kmst.cu",
+    "dcq": "src/FastWaveED_GPU3D_v1_DC_Earthquake/FastWaveED_GPU3D_v1.cu",
 }
 # The grid defines only size the host-side constants of the reference; every kernel takes
 # nx, ny, nz as arguments, so one build serves every grid.

@@ -18,6 +18,8 @@
  *                                   src/FastWaveED_GPU3D_v1_9km_station/FastWaveED_GPU3D_v1_9kmst.cu:287-331;
  *                                   its velocity update is ANISO's (9kmst.cu:333-388)
  *   linear velocity damping         src/FastWaveED_GPU3D_v1_16km_station/FastWaveED_GPU3D_v1_16kmst.cu:337-349
+ *   per-component 3-D weights       src/FastWaveED_GPU3D_v1_DC_Earthquake/FastWaveED_GPU3D_v1.cu:298-320 (stress),
+ *                                   :328-360 (velocity)
  *   receiver sampling               OK4 :383-386, ANISO :254-268
  *   time-loop order                 OK4 :485-505, ANISO :519-555
  *
@@ -40,6 +42,9 @@ typedef struct orc_grid {
     double c66;        /* isotropic shear modulus, scalar pa2[7] (OK4:405) */
     double bx, by, bz; /* isotropic buoyancy 1/rho, scalars pa3[0..2] (OK4:407) */
     double vdamp;      /* linear velocity damping (16 km scheme), 0 = off */
+    double c44, c55;   /* per-component-weight scheme: shear moduli of yz and xz (c66: xy) */
+    int32_t damping;   /* 3 = per-component weights (w[0..5]: Vx/sxx, Vy/syy, Vz/szz, sxy, sxz, syz) */
+    int32_t pad;
 } orc_grid;
 
 #define OT float
@@ -54,7 +59,7 @@ typedef struct orc_grid {
 #undef OT
 #undef OSUF
 
-int orc_abi_version(void) { return 2; }
+int orc_abi_version(void) { return 3; }
 
 int orc_num_threads(void)
 {

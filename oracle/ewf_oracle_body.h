@@ -92,6 +92,58 @@ static void OFN(stress_iso)(const orc_grid *g, OT *const *f, const OT *const *m,
     }
 }
 
+/* Isotropic stress update with a 3-D weight field per component (the DC_Earthquake solver,
+ * FastWaveED_GPU3D_v1.cu:298-320): w_c * (sigma_c + ...), each weight in its component's
+ * layout (w[0] Vx-, w[1] Vy-, w[2] Vz-, w[3..5] sxy/sxz/syz-shaped), shear moduli c66 (xy),
+ * c55 (xz), c44 (yz), shear cells guarded like ANISO. */
+static void OFN(stress_iso_percomp)(const orc_grid *g, OT *const *f, const OT *const *m, const OT *const *w)
+{
+    const long nx = g->nx, ny = g->ny, nz = g->nz;
+    const OT dt = (OT)g->dt, rdx = (OT)1.0 / (OT)g->dx, rdy = (OT)1.0 / (OT)g->dy, rdz = (OT)1.0 / (OT)g->dz;
+    const OT c66 = (OT)g->c66, c55 = (OT)g->c55, c44 = (OT)g->c44;
+    const OT *Vx = f[0], *Vy = f[1], *Vz = f[2];
+    OT *sxx = f[3], *syy = f[4], *szz = f[5], *sxy = f[6], *sxz = f[7], *syz = f[8];
+    const OT *c11 = m[0], *c12 = m[1];
+    long k;
+#pragma omp parallel for schedule(static)
+    for (k = 0; k < nz; k++) {
+        for (long j = 0; j < ny; j++) {
+            for (long i = 0; i < nx; i++) {
+                const long c = i + nx * (j + ny * k);
+                const long ex = i + (nx + 1) * (j + ny * k), ey = i + nx * (j + (ny + 1) * k);
+                const OT Vxx = (Vx[ex + 1] - Vx[ex]) * rdx;
+                const OT Vyy = (Vy[i + nx * ((j + 1) + (ny + 1) * k)] - Vy[ey]) * rdy;
+                const OT Vzz = (Vz[i + nx * (j + ny * (k + 1))] - Vz[c]) * rdz;
+                /* :313-315 */
+                sxx[c] = w[0][ex] * (sxx[c] + dt * (c11[c] * Vxx + c12[c] * Vyy + c12[c] * Vzz));
+                syy[c] = w[1][ey] * (syy[c] + dt * (c12[c] * Vxx + c11[c] * Vyy + c12[c] * Vzz));
+                szz[c] = w[2][c] * (szz[c] + dt * (c12[c] * Vxx + c12[c] * Vyy + c11[c] * Vzz));
+                /* :318 */
+                if (i > 0 && j > 0) {
+                    const long e = i + (nx + 1) * (j + (ny + 1) * k);
+                    const OT dvy = Vy[ey] - Vy[(i - 1) + nx * (j + (ny + 1) * k)];
+                    const OT dvx = Vx[ex] - Vx[i + (nx + 1) * ((j - 1) + ny * k)];
+                    sxy[e] = w[3][e] * (sxy[e] + c66 * dt * (dvy * rdx + dvx * rdy));
+                }
+                /* :319 */
+                if (i > 0 && k > 0) {
+                    const long e = ex;
+                    const OT dvz = Vz[c] - Vz[(i - 1) + nx * (j + ny * k)];
+                    const OT dvx = Vx[ex] - Vx[i + (nx + 1) * (j + ny * (k - 1))];
+                    sxz[e] = w[4][e] * (sxz[e] + c55 * dt * (dvz * rdx + dvx * rdz));
+                }
+                /* :320 */
+                if (j > 0 && k > 0) {
+                    const long e = ey;
+                    const OT dvy = Vy[ey] - Vy[i + nx * (j + (ny + 1) * (k - 1))];
+                    const OT dvz = Vz[c] - Vz[i + nx * ((j - 1) + ny * k)];
+                    syz[e] = w[5][e] * (syz[e] + c44 * dt * (dvy * rdz + dvz * rdy));
+                }
+            }
+        }
+    }
+}
+
 /* Orthorhombic stress update with a 3-D weight field (ANISO:287-356 compute_StressOrtho). */
 static void OFN(stress_ortho)(const orc_grid *g, OT *const *f, const OT *const *m, const OT *W)
 {
@@ -246,6 +298,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
     OT *Vx = f[0], *Vy = f[1], *Vz = f[2];
     const OT *sxx = f[3], *syy = f[4], *szz = f[5], *sxy = f[6], *sxz = f[7], *syz = f[8];
     const int iso = (g->model == 0);
+    const int pc = (g->damping == 3);  /* per-component weights, in each velocity's own layout */
     const OT bx = (OT)g->bx, by = (OT)g->by, bz = (OT)g->bz;
     const OT vd = (OT)g->vdamp;  /* 16kmst.cu:337-349: update - vdamp * V_old */
     long k;
@@ -261,7 +314,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
                                  + (sxy[i + (nx + 1) * ((j + 1) + (ny + 1) * k)] - sxy[i + (nx + 1) * (j + (ny + 1) * k)]) * rdy
                                  + (sxz[i + (nx + 1) * (j + ny * (k + 1))] - sxz[i + (nx + 1) * (j + ny * k)]) * rdz;
                     OT a, inc;
-                    if (iso) { a = w[0][i - 1]; }
+                    if (iso) { a = pc ? w[0][e] : w[0][i - 1]; }
                     else     { a = W[c]; }
                     if (!comp) {
                         if (iso) Vx[e] = a * (Vx[e] * rdt + bx * dSx) * dt;
@@ -283,7 +336,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
                                  + (sxy[(i + 1) + (nx + 1) * (j + (ny + 1) * k)] - sxy[i + (nx + 1) * (j + (ny + 1) * k)]) * rdx
                                  + (syz[i + nx * (j + (ny + 1) * (k + 1))] - syz[i + nx * (j + (ny + 1) * k)]) * rdz;
                     OT a, inc;
-                    if (iso) { a = w[1][j - 1]; }
+                    if (iso) { a = pc ? w[1][e] : w[1][j - 1]; }
                     else     { a = W[c]; }
                     if (!comp) {
                         if (iso) Vy[e] = a * (Vy[e] * rdt + by * dSy) * dt;
@@ -305,7 +358,7 @@ static void OFN(velocity)(const orc_grid *g, OT *const *f, const OT *const *m, c
                                  + (sxz[(i + 1) + (nx + 1) * (j + ny * k)] - sxz[i + (nx + 1) * (j + ny * k)]) * rdx
                                  + (syz[i + nx * ((j + 1) + (ny + 1) * k)] - syz[i + nx * (j + (ny + 1) * k)]) * rdy;
                     OT a, inc;
-                    if (iso) { a = w[2][k - 1]; }
+                    if (iso) { a = pc ? w[2][e] : w[2][k - 1]; }
                     else     { a = W[c]; }
                     if (!comp) {
                         if (iso) Vz[e] = a * (Vz[e] * rdt + bz * dSz) * dt;
@@ -348,6 +401,7 @@ int OFN(orc_run)(const orc_grid *g, OT *const *f, OT *const *comp, const OT *con
     if (it0 < 0 || nsteps < 0 || it0 + nsteps > nstf) return -2;
     if (nrec > 0 && it0 + nsteps > trace_len) return -3;
     if (g->model == 0 && (!w || !w[0] || !w[1] || !w[2])) return -4;
+    if (g->damping == 3 && (g->model != 0 || !w[3] || !w[4] || !w[5])) return -11;
     if (g->model != 0 && !W) return -5;
     if (g->model < 0 || g->model > 2) return -10;
     for (int32_t s = 0; s < nsrc; s++) {
@@ -372,7 +426,8 @@ int OFN(orc_run)(const orc_grid *g, OT *const *f, OT *const *comp, const OT *con
     }
     for (int32_t s = 0; s < nsteps; s++) {
         const int it = it0 + s;
-        if (g->model == 0)      OFN(stress_iso)(g, f, m, w);
+        if (g->model == 0 && g->damping == 3) OFN(stress_iso_percomp)(g, f, m, w);
+        else if (g->model == 0) OFN(stress_iso)(g, f, m, w);
         else if (g->model == 2) OFN(stress_isohet)(g, f, m, W);
         else                    OFN(stress_ortho)(g, f, m, W);
         if (g->src_order == 0) OFN(inject)(g, f, nsrc, src, coef, stf, it);

@@ -23,7 +23,8 @@ class Grid(C.Structure):
                 ("src_order", C.c_int32), ("bc1_rows", C.c_int32),
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
                 ("c66", C.c_double), ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
-                ("vdamp", C.c_double)]
+                ("vdamp", C.c_double), ("c44", C.c_double), ("c55", C.c_double), ("damping", C.c_int32),
+                ("pad", C.c_int32)]
 
 
 _lib = None
@@ -87,11 +88,13 @@ class Runner:
                 state.comp = [np.zeros(F.shape(q, m.nx, m.ny, m.nz), dtype) for q in (F.F_VX, F.F_VY, F.F_VZ)]
         self.state = state
         self.grid = Grid(m.nx, m.ny, m.nz, m.model, m.src_order, bc1_rows(m), m.dx, m.dy, m.dz, m.dt, m.c66, m.bx,
-                         m.by, m.bz, getattr(m, "vdamp", 0.0))
+                         m.by, m.bz, getattr(m, "vdamp", 0.0), getattr(m, "c44", 0.0), getattr(m, "c55", 0.0),
+                         m.damping, 0)
         cv = lambda a: np.ascontiguousarray(a, dtype=dtype)  # noqa: E731
         if m.model == F.MODEL_ISO:
             self.mats = [cv(m.materials[F.M_C11]), cv(m.materials[F.M_C12])]
-            self.w = [cv(m.damping_arrays[k]) for k in (F.D_WX, F.D_WY, F.D_WZ)]
+            keys = F.PERCOMP_WEIGHTS if m.damping == F.DAMP_PERCOMP else (F.D_WX, F.D_WY, F.D_WZ)
+            self.w = [cv(m.damping_arrays[k]) for k in keys]
             self.W = None
         else:
             # orthorhombic slots; the 9 km scheme leaves C22, C33, C13, C23 empty

@@ -8,6 +8,7 @@ FastWaveED_GPU3D_v1_9kmst_ANISO.cu:391-608): allocation, the launch geometry
   isotropic:     compute_StressPrf, BC1, update_Qxft                    (OK4:485-505)
   orthorhombic:  compute_StressOrtho, BC1, source, update_VelocityFromStress (ANISO:519-555)
   9 km / 16 km:  compute_StressPrf, BC1, source, update_Qxft            (9kmst.cu:463-477)
+  DC_Earthquake: compute_StressPrf, BC1, source, update_Qxft            (FastWaveED_GPU3D_v1.cu:473-483)
 with our receivers gathered from V after each step (a read-only gather; the reference's own
 hard-coded `record` cells are left as they are).
 
@@ -59,13 +60,16 @@ def _ck(st: int, what: str) -> None:
         raise RuntimeError(f"{what}: {lib().refk_error().decode(errors='replace')}")
 
 
-def cubin(model: int, variant: str, vdamp: float = 0.0) -> str:
-    name = {F.MODEL_ISO: "ok4", F.MODEL_ORTHO: "aniso"}.get(model, "iso16km" if vdamp else "iso9km")
+def cubin(model: int, variant: str, vdamp: float = 0.0, damping: int = -1) -> str:
+    if model == F.MODEL_ISO and damping == F.DAMP_PERCOMP:
+        name = "dcq"
+    else:
+        name = {F.MODEL_ISO: "ok4", F.MODEL_ORTHO: "aniso"}.get(model, "iso16km" if vdamp else "iso9km")
     return os.path.join(HERE, "_ref", f"{name}_{variant}.cubin")
 
 
-def available(model: int = F.MODEL_ISO, variant: str = "exact", vdamp: float = 0.0) -> bool:
-    return os.path.exists(cubin(model, variant, vdamp))
+def available(model: int = F.MODEL_ISO, variant: str = "exact", vdamp: float = 0.0, damping: int = -1) -> bool:
+    return os.path.exists(cubin(model, variant, vdamp, damping))
 
 
 class _Args:
@@ -100,7 +104,8 @@ class RefRunner:
         torch.zeros(1, device=self.dev)
         _ck(lib().refk_init(device), "refk_init")
         mod = C.c_void_p()
-        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant, getattr(m, "vdamp", 0.0))), C.byref(mod)), "refk_load")
+        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant, getattr(m, "vdamp", 0.0), m.damping)), C.byref(mod)),
+            "refk_load")
         self.mod = mod
         nx, ny, nz = m.nx, m.ny, m.nz
         self.pad = (nx + 2) * (ny + 2) + 64
@@ -170,7 +175,47 @@ class RefRunner:
         f = self.f
         nx, ny, nz = m.nx, m.ny, m.nz
         d = self.dummy
-        if m.model == F.MODEL_ISO:
+        if m.model == F.MODEL_ISO and m.damping == F.DAMP_PERCOMP:
+            if m.src_order != F.SRC_AFTER_BC1:
+                raise ValueError("DC_Earthquake reference = after-BC1 injection")
+            xs, ys, zs = self._check_sources(1)
+            coef = tuple(float(np.float32(v)) for v in self._mt_tuple())
+            if coef != F.DCQ_LEGACY_MT:
+                raise ValueError("the DC_Earthquake reference hard-codes its source: use fields.DCQ_LEGACY_MT")
+            c11 = self._upload(m.materials[F.M_C11])
+            c12 = self._upload(m.materials[F.M_C12])
+            # every weight field at its full extent (its driver writes them so), which keeps the
+            # kernels' edge-pitch reads of the shear weights inside the arrays
+            wx, wy, wz, wxy, wxz, wyz = (self._upload(m.damping_arrays[k]) for k in F.PERCOMP_WEIGHTS)
+            # compute_StressPrf(Prf, 6 stresses, Vx, Vy, Vz, Qxft, Qyft, Qzft, c11u_het, c12u_het,
+            # weights_x/y/z/xy/xz/yz, dx, dy, dz, dt, c11u c22u c33u c12u c13u c23u c44u c55u c66u,
+            # alpha1-3, M1, nx, ny, nz) (FastWaveED_GPU3D_v1.cu:298)
+            self.k_stress = self._fn("_Z17compute_StressPrf")
+            self.a_stress = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 3
+                + [("p", P(x)) for x in (c11, c12, wx, wy, wz, wxy, wxz, wyz)]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 6
+                + [("f", m.c44), ("f", m.c55), ("f", m.c66)] + [("f", 0.0)] * 4
+                + [("i", nx), ("i", ny), ("i", nz)])
+            self.it_pos_stress = None
+            self.k_src = self._fn("_Z6source")
+            self.a_src = _Args(
+                [("p", P(d))] * 4 + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1)] + [("p", P(d))] * 2
+                + [("p", P(self.src))] + [("f", m.dx), ("f", m.dy), ("f", m.dz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)]
+                + [("f", m.dt)])
+            self.it_pos_src = 15 + 9 + 3
+            # update_Qxft(Prf, 6 stresses, Vx, Vy, Vz, Qxft..Qzold (6), vrhox11het, weights_x/y/z,
+            # dx, dy, dz, dt, eta_k1-3, vrho_x/y/z_11, 6 unused, nx, ny, nz, chi) (:328)
+            self.k_vel = self._fn("_Z11update_Qxft")
+            self.a_vel = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 7
+                + [("p", P(x)) for x in (wx, wy, wz)]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 3
+                + [("f", m.bx), ("f", m.by), ("f", m.bz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5)])
+            self.it_pos_vel = None
+        elif m.model == F.MODEL_ISO:
             if m.src_order != F.SRC_BEFORE_BC1 or m.damping != F.DAMP_PML1D:
                 raise ValueError("isotropic reference = before-BC1 injection and 1-D PML")
             xs, ys, zs = self._check_sources(0)

@@ -69,8 +69,14 @@ def case_iso16km():
     return m
 
 
+def case_dcq():
+    m = I.random_small(F.MODEL_ISO, 14, 16, 12, nt=40, seed=108, damping=F.DAMP_PERCOMP)
+    m.set_moment_tensor(np.array(F.DCQ_LEGACY_MT), 5, 6, 3, 1)
+    return m
+
+
 CASES = {"ok4": case_ok4, "ok4_surface": case_ok4_surface, "aniso": case_aniso, "aniso_surface": case_aniso_surface,
-         "iso9km": case_iso9km, "iso9km_surface": case_iso9km_surface, "iso16km": case_iso16km}
+         "iso9km": case_iso9km, "iso9km_surface": case_iso9km_surface, "iso16km": case_iso16km, "dcq": case_dcq}
 
 
 def input_digest(m) -> str:
@@ -83,6 +89,8 @@ def input_digest(m) -> str:
     h.update(np.array([m.dx, m.dy, m.dz, m.dt, m.c66, m.bx, m.by, m.bz]).tobytes())
     if getattr(m, "vdamp", 0.0):
         h.update(np.array([m.vdamp]).tobytes())
+    if m.damping == F.DAMP_PERCOMP:
+        h.update(np.array([m.c44, m.c55]).tobytes())
     return h.hexdigest()
 
 

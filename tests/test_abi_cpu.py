@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 def test_abi_version_and_strerror(built_lib):
     lib = S.load_library()
-    assert lib.ewf_abi_version() == 2
+    assert lib.ewf_abi_version() == 3
     for code, name in F.STATUS.items():
         assert lib.ewf_strerror(code)
     assert lib.ewf_strerror(-99) == b"unknown status"
@@ -46,7 +46,7 @@ def test_params_struct_layout(built_lib):
     p = S.default_params()
     assert p.model == F.MODEL_ISO and p.precision == F.PREC_F32 and p.check_finite == 1
     assert p.fused == 0
-    assert C.sizeof(S.Params) == 14 * 4 + 9 * 8 + 8
+    assert C.sizeof(S.Params) == 14 * 4 + 11 * 8 + 8
 
 
 def _have_gpu():

@@ -76,6 +76,15 @@ def test_isohet_bitwise_vs_oracle(cuda_device, name, damping, nx, ny, nz, prec):
     assert_bitwise(product(m, 48, prec), ref, name)
 
 
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
+@pytest.mark.parametrize("nx,ny,nz", [(35, 40, 21), (29, 30, 27)])
+def test_percomp_bitwise_vs_oracle(cuda_device, prec, nx, ny, nz):
+    """The DC_Earthquake form: isotropic, one 3-D weight field per component, three shear moduli."""
+    m = I.random_small(F.MODEL_ISO, nx, ny, nz, nt=48, seed=nx + 3 * nz, damping=F.DAMP_PERCOMP)
+    ref = O.run(m, 48, prec)
+    assert_bitwise(product(m, 48, prec), ref, "percomp")
+
+
 @pytest.mark.parametrize("model", [F.MODEL_ORTHO, F.MODEL_ISO_HET], ids=["ortho", "isohet"])
 @pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F64], ids=["f32", "f64"])
 def test_velocity_damping_bitwise_vs_oracle(cuda_device, model, prec):

@@ -37,8 +37,8 @@ def edge_mask(q, shape):
 
 def reference(m, nsteps, variant):
     vd = getattr(m, "vdamp", 0.0)
-    assert R.available(m.model, variant, vd), \
-        f"missing {R.cubin(m.model, variant, vd)}: run oracle/build.py where the reference is"
+    assert R.available(m.model, variant, vd, m.damping), \
+        f"missing {R.cubin(m.model, variant, vd, m.damping)}: run oracle/build.py where the reference is"
     r = R.RefRunner(m, variant)
     try:
         r.run(nsteps)
@@ -68,11 +68,19 @@ def isohet_case(nx=36, ny=40, nz=26, nt=60, seed=23, zs=8, damping=F.DAMP_W3D, v
     return m
 
 
+def dcq_case(nx=36, ny=40, nz=26, nt=60, seed=25, zs=8):
+    """The DC_Earthquake solver: isotropic with per-component 3-D weights and its own source."""
+    m = I.random_small(F.MODEL_ISO, nx, ny, nz, nt=nt, seed=seed, damping=F.DAMP_PERCOMP)
+    m.set_moment_tensor(np.array(F.DCQ_LEGACY_MT), nx // 2 - 2, ny // 2 - 2, zs, 1)
+    return m
+
+
 @pytest.mark.parametrize("make", [iso_case, ortho_case, lambda: iso_case(zs=1), lambda: ortho_case(zs=0),
                                   lambda: ortho_case(damping=F.DAMP_SEPARABLE), isohet_case,
-                                  lambda: isohet_case(zs=0, damping=F.DAMP_SEPARABLE), lambda: isohet_case(vdamp=True)],
+                                  lambda: isohet_case(zs=0, damping=F.DAMP_SEPARABLE), lambda: isohet_case(vdamp=True),
+                                  dcq_case, lambda: dcq_case(zs=1)],
                          ids=["iso", "ortho", "iso-surface-src", "ortho-surface-src", "ortho-separable", "iso9km",
-                              "iso9km-surface-separable", "iso16km"])
+                              "iso9km-surface-separable", "iso16km", "dcq", "dcq-surface-src"])
 def test_product_bitwise_vs_reference_exact(cuda_device, make):
     m = make()
     rf, rt = reference(m, m.nt, "exact")
@@ -89,7 +97,7 @@ def test_product_bitwise_vs_reference_exact(cuda_device, make):
     assert np.abs(rt).max() > 0
 
 
-@pytest.mark.parametrize("model", [F.MODEL_ISO, F.MODEL_ORTHO, F.MODEL_ISO_HET])
+@pytest.mark.parametrize("model", [F.MODEL_ISO, F.MODEL_ORTHO, F.MODEL_ISO_HET, -1], ids=["iso", "ortho", "iso16km", "dcq"])
 def test_seismograms_vs_reference_stock_build(cuda_device, model):
     """North-star criterion: relative L2 seismogram error <= 1e-4 against the reference built with
     its own flags (FMA contraction on), after the full run."""
@@ -101,8 +109,10 @@ def test_seismograms_vs_reference_stock_build(cuda_device, model):
         m = I.ortho_layered(nx=64, ny=64, nz=48, nt=400, src=(32, 32, 12), rec_coords=[8, 20, 32, 44, 56],
                             damping=F.DAMP_W3D)
         m.set_moment_tensor(np.array(F.ANISO_LEGACY_MT), 31, 31, 11, 1)
-    else:
+    elif model == F.MODEL_ISO_HET:
         m = isohet_case(nx=64, ny=64, nz=48, nt=400, seed=24, zs=11, vdamp=True)
+    else:
+        m = dcq_case(nx=64, ny=64, nz=48, nt=400, seed=26, zs=11)
     _, rt = reference(m, m.nt, "stock")
     with Solver.from_model(m) as s:
         s.run(m.nt)
