@@ -77,6 +77,67 @@ def pml_factors(n: int, lpml: int, dt: float, R: float = 1e-8, sides: str = "bot
     return pml_weights(n, lpml, dt, R, sides=sides)[:n].copy()
 
 
+def percomp_weights(nx: int, ny: int, nz: int, dt: float, lpml: int = 110, R: float = 1e-5) -> dict:
+    """The DC_Earthquake driver's per-component weights (vizme_FastWaveED_GPU3D.m:293-358), keyed by
+    the EWF_D_P* field ids, in the components' layouts.
+
+    sigma_i = 1.5/(lpml/nx) log10(1/R) ((lpml - i + 1)/lpml)^2 on the first lpml cells of every
+    axis and mirrored at the far end (the driver uses nx for all three axes); normal weights are
+    exp(-sigma dt) on both x and y ends and the bottom z end (free surface on top); the shear
+    weights exp(-(sigma_a + sigma_b) dt / 2) are painted by the driver's double loop, whose
+    overlapping assignments are replayed here in the same order (1-based MATLAB indices moved to
+    0-based; each shear pattern is constant along its third axis)."""
+    pw = lpml
+    if min(nx, ny, nz) <= 2 * pw + 2:
+        raise ValueError(f"grid {nx}x{ny}x{nz} too small for lpml {lpml}")
+    i_vec = np.arange(1, pw + 1, dtype=np.float64)
+    sigma = 3 * 1 / 2 / (pw / nx) * math.log10(1 / R) * ((pw - i_vec + 1) / pw) ** 2
+    px, py, pz = np.zeros(nx), np.zeros(ny), np.zeros(nz)
+    for a, n in ((px, nx), (py, ny), (pz, nz)):
+        a[:pw] = sigma
+        a[n - pw:] = sigma[::-1]
+    dfx, dfy, dfz = (np.exp(-a[:pw] * dt) for a in (px, py, pz))
+    wx = np.ones((nz, ny, nx + 1))
+    wx[:, :, :pw] = dfx
+    wx[:, :, nx + 1 - pw:] = dfx[::-1]
+    wy = np.ones((nz, ny + 1, nx))
+    wy[:, :pw, :] = dfy[None, :, None]
+    wy[:, ny + 1 - pw:, :] = dfy[::-1][None, :, None]
+    wz = np.ones((nz + 1, ny, nx))
+    wz[nz + 1 - pw:, :, :] = dfz[::-1][:, None, None]
+    xy = np.ones((ny + 1, nx + 1))   # [y, x], every z
+    xz = np.ones((nz + 1, nx + 1))   # [z, x], every y
+    yz = np.ones((nz + 1, ny + 1))   # [z, y], every x
+    for i in range(1, pw + 1):
+        for j in range(1, pw + 1):
+            dxy = math.exp(-0.5 * (px[i - 1] + py[j - 1]) * dt)
+            dxz = math.exp(-0.5 * (px[i - 1] + pz[j - 1]) * dt)
+            dyz = math.exp(-0.5 * (py[i - 1] + pz[j - 1]) * dt)
+            xy[pw - 1:ny + 1 - pw, i - 1] = dxy
+            xy[j - 1, pw - 1:nx + 1 - pw] = dxy
+            xy[j - 1, i - 1] = dxy
+            xy[pw - 1:ny + 1 - pw, nx - i - 1] = dxy
+            xy[ny - j - 1, pw - 1:nx + 1 - pw] = dxy
+            xy[ny - j - 1, nx - i - 1] = dxy
+            xy[j - 1:pw, nx - i - 1] = dxy
+            xy[ny - j - 1, i - 1:pw] = dxy
+            xz[0:nz + 1 - pw, i - 1] = dxz
+            xz[0:nz + 1 - pw, nx - i - 1] = dxz
+            xz[nz - j - 1, pw - 1:nx + 1 - pw] = dxz
+            xz[nz - j - 1, nx - i - 1] = dxz
+            xz[nz - j - 1, i - 1:pw] = dxz
+            yz[0:nz + 1 - pw, i - 1] = dyz
+            yz[0:nz + 1 - pw, ny - i - 1] = dyz
+            yz[nz - j - 1, pw - 1:ny + 1 - pw] = dyz
+            yz[nz - j - 1, ny - i - 1] = dyz
+            yz[nz - j - 1, i - 1:pw] = dyz
+    f32 = lambda a: np.ascontiguousarray(a, dtype=np.float32)  # noqa: E731
+    return {F.D_PX: f32(wx), F.D_PY: f32(wy), F.D_PZ: f32(wz),
+            F.D_PXY: f32(np.broadcast_to(xy[None, :, :], (nz, ny + 1, nx + 1))),
+            F.D_PXZ: f32(np.broadcast_to(xz[:, None, :], (nz + 1, ny, nx + 1))),
+            F.D_PYZ: f32(np.broadcast_to(yz[:, :, None], (nz + 1, ny + 1, nx)))}
+
+
 # ---------------------------------------------------------------------------------------------
 # materials
 # ---------------------------------------------------------------------------------------------

@@ -2,6 +2,7 @@
 import math
 
 import numpy as np
+import pytest
 
 from elanfmt_gb300 import fields as F
 from elanfmt_gb300 import inputs as I
@@ -201,3 +202,23 @@ def test_iso_het_layered_fields():
     assert bz.shape == (15, 10, 12) and bz[0].max() == 0 and np.isclose(bz[6, 3, 3], (1 / 2200 + 1 / 2700) / 2)
     w = m.damping_arrays[F.D_W3D]
     assert w.shape == (14, 10, 12) and w[0, 5, 6] == 1.0 and w[-1, 5, 6] < 1.0
+
+
+def test_percomp_weights_follow_the_driver():
+    nx, ny, nz, lpml, dt = 30, 28, 26, 6, 0.002
+    w = I.percomp_weights(nx, ny, nz, dt, lpml=lpml)
+    for fid, arr in w.items():
+        assert arr.shape == F.shape(fid, nx, ny, nz) and arr.dtype == np.float32
+        assert arr.max() <= 1.0 and arr.min() > 0.0
+    sig1 = 1.5 / (lpml / nx) * 5.0  # log10(1/1e-5) = 5, the outermost cell
+    assert np.isclose(w[F.D_PX][3, 4, 0], np.exp(-sig1 * dt))
+    assert w[F.D_PX][3, 4, nx // 2] == 1.0
+    assert np.isclose(w[F.D_PX][3, 4, nx], np.exp(-sig1 * dt))           # mirrored at the far end
+    assert w[F.D_PZ][0, 5, 5] == 1.0 and w[F.D_PZ][nz, 5, 5] < 1.0        # no damping at the top
+    # shear weights: the corner cell carries the mean of both profiles; the interior is untouched
+    assert np.isclose(w[F.D_PXY][7, 0, 0], np.exp(-sig1 * dt))
+    assert w[F.D_PXY][7, ny // 2, nx // 2] == 1.0
+    assert np.all(w[F.D_PXY] == w[F.D_PXY][:1])                           # constant along z
+    assert np.all(w[F.D_PYZ] == w[F.D_PYZ][:, :, :1])                     # constant along x
+    with pytest.raises(ValueError):
+        I.percomp_weights(12, 12, 12, dt, lpml=6)
