@@ -146,7 +146,7 @@ __device__ __forceinline__ int inject_when(const StepArgs<T> &a, const SrcEntry 
 }
 
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-__global__ void __launch_bounds__(FX * FY, 2) k_step(const FusedArgs<T> fa)
+__global__ void __launch_bounds__(FX * FY, 3) k_step(const FusedArgs<T> fa)
 {
     const StepArgs<T> &a = fa.a;
     __shared__ T s_xx[2][FY][FX + 1];      // col 0: i0-1, col tx+1: own
