@@ -1,0 +1,75 @@
+"""Cache of the z-chunk autotuner's choices (JSON), so a workload is timed once per GPU model.
+
+The library's autotuner (`ewf_autotune`, `ewf_batch_autotune`) times the step for z-chunks of
+4..64 planes.  The best chunk depends on the GPU, the scheme (model, damping, precision, one-pass
+or two-kernel step) and the grid, not on the inputs' values, so it is stored under that key:
+
+    from elanfmt_gb300 import tuning
+    k = tuning.kchunk_for(model, precision=F.PREC_F32)      # cached, or tuned once and stored
+    with Solver.from_model(model, kchunk=k) as s: ...
+
+The cache file defaults to $EWF_TUNING_CACHE or ~/.cache/elanfmt_gb300/kchunk.json.
+"""
+from __future__ import annotations
+
+import json
+import os
+import tempfile
+
+from . import fields as F
+
+
+def cache_path() -> str:
+    return os.environ.get("EWF_TUNING_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "elanfmt_gb300",
+                                                              "kchunk.json")
+
+
+def key(device_name: str, m, precision: int, fused: bool) -> str:
+    return (f"{device_name}|model{m.model}|damp{m.damping}|prec{precision}|{'fused' if fused else 'split'}|"
+            f"{m.nx}x{m.ny}x{m.nz}")
+
+
+def load(path: str | None = None) -> dict:
+    p = path or cache_path()
+    try:
+        with open(p) as fh:
+            data = json.load(fh)
+        return data if isinstance(data, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def store(k: str, kchunk: int, path: str | None = None) -> None:
+    """Adds one entry; the file is replaced atomically so concurrent writers never leave it torn."""
+    p = path or cache_path()
+    data = load(p)
+    data[k] = int(kchunk)
+    os.makedirs(os.path.dirname(p) or ".", exist_ok=True)
+    fd, tmp = tempfile.mkstemp(dir=os.path.dirname(p) or ".", suffix=".tmp")
+    with os.fdopen(fd, "w") as fh:
+        json.dump(data, fh, indent=1, sort_keys=True)
+    os.replace(tmp, p)
+
+
+def kchunk_for(m, precision: int = F.PREC_F32, fused: bool = False, nsteps: int = 30, path: str | None = None,
+               device_name: str | None = None, tune=None) -> int:
+    """The cached z-chunk for this workload shape, or the autotuner's choice (then cached).
+    `tune(m, precision, fused, nsteps) -> int` replaces the GPU autotuner (tests)."""
+    if device_name is None:
+        import torch
+
+        device_name = torch.cuda.get_device_name()
+    k = key(device_name, m, precision, fused)
+    data = load(path)
+    if k in data:
+        return int(data[k])
+    if tune is None:
+        from .solver import Solver
+
+        def tune(m_, p_, f_, n_):
+            with Solver.from_model(m_, precision=p_, fused=f_) as s:
+                return s.autotune(n_)
+
+    best = int(tune(m, precision, fused, nsteps))
+    store(k, best, path)
+    return best
