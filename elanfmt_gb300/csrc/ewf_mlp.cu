@@ -1,7 +1,7 @@
 // ewf_mlp.cu -- kernels of the learned Green's-function surrogate (training and inference).
 //
 // A small MLP maps (source x, y, depth, receiver offset, azimuth) to the 6 x 3 x nt elementary
-// Green's-function seismograms; the solver generates its training data and judges its error.
+// Green's-function seismograms; the solver generates its training data and measures its error.
 // Everything here works on caller-owned device buffers (plain pointers):
 //   ewf_mlp_gemm        C[M,N] = A[M,K] . B[N,K]^T (+ bias), bf16 operands on the tensor cores
 //                       (mma.sync m16n8k16, fp32 accumulation), epilogue: fp32 out, bf16 out,

@@ -1,12 +1,14 @@
 """Learned Green's-function surrogate: data from the batched solver, an MLP trained and run by the
-project's own CUDA kernels (ewf_mlp_*), the solver as fallback and judge.
+project's own CUDA kernels (ewf_mlp_*), the solver as fallback and as the measure of its error.
 
-Network: (source depth, receiver offset, first and second azimuthal harmonics) -> 6 elementary
-moment tensors x 3 velocity components x nt samples, 4 hidden layers of 512 GELU units, bf16
-weights and activations, fp32 accumulation (tensor cores), fp32 master weights and Adam.  The
-model is laterally homogeneous, so the source's x and y enter only through offset and azimuth.
-torch only holds the device buffers; every arithmetic op of training and inference is one of the
-hand-written kernels in csrc/ewf_mlp.cu.
+Network (default, "structured"): (source depth, receiver offset) -> the 10 fundamental traces
+of a point moment tensor in a laterally homogeneous medium, which ewf_mlp_combine mixes into the
+6 elementary moment tensors x 3 velocity components for the query's azimuth
+(mixing_matrices); the other form maps (depth, offset, first and second azimuthal harmonics) to
+the 18 traces directly.  4 hidden layers of 512 GELU units, bf16 weights and activations, fp32
+accumulation (tensor cores), fp32 master weights and Adam.  torch only holds the device buffers;
+every arithmetic op of training and inference is one of the hand-written kernels in
+csrc/ewf_mlp.cu.
 
     python -m elanfmt_gb300.surrogate [--train-runs 256] [--test-runs 64] [--out report.json]
 """
@@ -393,8 +395,8 @@ def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: i
 
 def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 512, layers: int = 4,
                      lr: float = 1e-3, spreading: bool = True, structured: bool = True, log=print) -> dict:
-    """Trains the MLP on the training sources of a dataset and judges it on the held-out ones
-    against the solver's traces; also judges the nearest-neighbour method (no network) and the
+    """Trains the MLP on the training sources of a dataset and scores it on the held-out ones
+    against the solver's traces; also scores the nearest-neighbour method (no network) and the
     fallback policy.  structured: the network maps (depth, offset) to the 10 fundamental traces
     and ewf_mlp_combine mixes them into the 18 traces of each receiver's azimuth; otherwise it maps
     (depth, offset, azimuth harmonics) to the 18 traces directly."""
