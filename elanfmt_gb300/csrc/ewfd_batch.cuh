@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(TX * TY, 4) k_bvelocity(const BatchProb<T> *__
 // so the R CTAs of a tile are dispatched together and read the tile's material planes from HBM
 // once (the other R-1 reads hit L2).
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY) k_stress_mr(const StepArgs<T> a, int R, long long rhs_stride)
+__global__ void __launch_bounds__(TX * TY, 4) k_stress_mr(const StepArgs<T> a, int R, long long rhs_stride)
 {
     const int r = blockIdx.x % R;
     const int tx = blockIdx.x / R;
@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(TX * TY) k_stress_mr(const StepArgs<T> a, int 
 }
 
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY) k_velocity_mr(const StepArgs<T> a, int R, long long rhs_stride)
+__global__ void __launch_bounds__(TX * TY, 4) k_velocity_mr(const StepArgs<T> a, int R, long long rhs_stride)
 {
     const int r = blockIdx.x % R;
     const int tx = blockIdx.x / R;

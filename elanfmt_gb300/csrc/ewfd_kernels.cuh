@@ -271,7 +271,7 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
 }
 
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY) k_stress(const StepArgs<T> a)
+__global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 4 : 1) k_stress(const StepArgs<T> a)
 {
     const int k0 = blockIdx.z * a.kchunk;
     stress_column<T, MODEL, DAMP, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
