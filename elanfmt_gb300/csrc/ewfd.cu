@@ -1072,12 +1072,15 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     h->it += nsteps;
     if (h->p.check_finite && h->nrec > 0 && nsteps > 0) {
-        std::vector<double> tr((size_t)h->nrec * h->p.nt);
-        CK(cudaMemcpy(tr.data(), h->d_traces, tr.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        // only the samples of this call: columns [it - nsteps, it) of the nrec x nt traces
+        const int t0 = h->it - nsteps;
+        std::vector<double> tr((size_t)h->nrec * nsteps);
+        CK(cudaMemcpy2D(tr.data(), (size_t)nsteps * sizeof(double), h->d_traces + t0, (size_t)h->p.nt * sizeof(double),
+                        (size_t)nsteps * sizeof(double), (size_t)h->nrec, cudaMemcpyDeviceToHost));
         for (int r = 0; r < h->nrec; ++r)
-            for (int t = h->it - nsteps; t < h->it; ++t)
-                if (!std::isfinite(tr[(size_t)r * h->p.nt + t]))
-                    return ewf_fail(EWF_ERR_NONFINITE, "receiver %d has a non-finite sample at step %d", r, t);
+            for (int t = 0; t < nsteps; ++t)
+                if (!std::isfinite(tr[(size_t)r * nsteps + t]))
+                    return ewf_fail(EWF_ERR_NONFINITE, "receiver %d has a non-finite sample at step %d", r, t0 + t);
     }
     return EWF_OK;
 }

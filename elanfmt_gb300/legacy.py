@@ -28,7 +28,8 @@ def write_inputs(m, workdir: str) -> None:
     Lx, Ly, Lz = (m.nx - 1) * m.dx, (m.ny - 1) * m.dy, (m.nz - 1) * m.dz
     _w(j("pa1.dat"), [m.dx, m.dy, m.dz, m.dt, Lx, Ly, Lz, Lx / 10, Ly / 10, Lz / 10])
     c66 = m.c66
-    _w(j("pa2.dat"), [0, 0, 0, 0, 0, 0, 0, c66, 0, 0, 0, 0, 0])
+    # pa2 = [c11u c33u c13u c12u c23u c44u c55u c66u ...] (OK4:402, 405)
+    _w(j("pa2.dat"), [0, 0, 0, 0, 0, getattr(m, "c44", 0.0), getattr(m, "c55", 0.0), c66, 0, 0, 0, 0, 0])
     _w(j("pa3.dat"), [m.bx, m.by, m.bz] + [0.0] * 9)
     mt = np.zeros(6)
     if m.sources is not None:

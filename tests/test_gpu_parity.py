@@ -204,6 +204,20 @@ def test_errors_are_status_codes(cuda_device):
         with pytest.raises(EwfError) as e:
             s.run(10)
         assert e.value.status == -7  # non-finite traces detected on the host
+    with Solver.from_model(m, check_finite=False) as s:
+        s.run(10)
+        tr = s.seismograms()
+    bad = ~np.isfinite(tr)
+    t_star = int(np.nonzero(bad.any(axis=0))[0][0])  # first step with a non-finite sample
+    if t_star > 0:  # the check covers the samples of each call: a later call reports them
+        r0 = int(np.nonzero(bad[:, t_star:].any(axis=1))[0][0])
+        t0 = t_star + int(np.nonzero(bad[r0, t_star:])[0][0])
+        with Solver.from_model(m) as s:
+            s.run(t_star)
+            with pytest.raises(EwfError) as e:
+                s.run(10 - t_star)
+            assert e.value.status == -7
+            assert f"receiver {r0} has a non-finite sample at step {t0}" in str(e.value)
     # inputs missing
     with Solver.from_model(I.random_small(F.MODEL_ISO, 20, 20, 16, nt=10, seed=1)) as s0:
         params = s0.params
@@ -248,6 +262,32 @@ def test_legacy_file_contract_through_ewfd(cuda_device, tmp_path):
         np.testing.assert_array_equal(s.seismograms(), ref.traces)
     finally:
         s.close()
+
+
+@pytest.mark.parametrize("flag,model,damping", [("ortho", F.MODEL_ORTHO, F.DAMP_W3D),
+                                                ("isohet", F.MODEL_ISO_HET, F.DAMP_W3D),
+                                                ("dcq", F.MODEL_ISO, F.DAMP_PERCOMP)])
+def test_legacy_file_contract_other_schemes(cuda_device, tmp_path, flag, model, damping):
+    """The orthorhombic, 9 km and DC_Earthquake file sets through `ewfd --model ...`."""
+    m = I.random_small(model, 40, 44, 24, nt=40, seed=19, damping=damping)
+    xs, ys, zs = 12, 13, 9
+    m.set_moment_tensor(np.array([0.5, -1.0, 0.3, 0.2, 1.0, 0.8]), xs, ys, zs, 1)
+    m.receivers = np.array([[30, 20, 1, F.F_VZ], [30, 20, 1, F.F_VX], [30, 23, 1, F.F_VY], [30, 22, 1, F.F_VY],
+                            [5, 6, 7, F.F_VZ]], np.int32)
+    L.write_inputs(m, str(tmp_path))
+    with open(tmp_path / "rec.txt", "w") as fh:
+        for r in m.receivers:
+            fh.write(" ".join(str(int(v)) for v in r) + "\n")
+    exe = os.path.join(ROOT, "elanfmt_gb300", "ewfd")
+    r = subprocess.run([exe, "--nx", "40", "--ny", "44", "--nz", "24", "--model", flag, "--workdir", str(tmp_path),
+                        "--src", f"{xs},{ys},{zs}", "--receivers", str(tmp_path / "rec.txt"), "--quiet"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = L.read_outputs(str(tmp_path), m.nt)
+    ref = O.run(m, 40)
+    for q, name in ((F.F_VX, "Vx"), (F.F_VY, "Vy"), (F.F_VZ, "Vz")):
+        np.testing.assert_array_equal(out[name], ref.f[q])
+    np.testing.assert_array_equal(out["Rec_all"], ref.traces.astype(np.float32))
 
 
 def test_async_snapshots_are_the_fields_at_their_step(cuda_device, tmp_path):
