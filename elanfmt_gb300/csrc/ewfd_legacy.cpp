@@ -219,9 +219,12 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
         stencil = 0;
     } else {
         // ANISO (and the 9 km scheme, 9kmst.cu:228-246) hard-code the tensor in their source
-        // kernel (ANISO:233-247): xx yy zz xy xz yz
-        const float c[6] = {-0.6282f, 0.9437f, 0.2439f, 0.4455f, -0.2709f, -0.2362f};
-        for (int q = 0; q < 6; ++q) mt[q] = c[q];
+        // kernel (ANISO:233-247): xx yy zz xy xz yz; the 16 km scheme (the 9 km one with vdamp)
+        // another one in the same kernel (16kmst.cu:228-252)
+        const float c9[6] = {-0.6282f, 0.9437f, 0.2439f, 0.4455f, -0.2709f, -0.2362f};
+        const float c16[6] = {-0.7448f, 1.0603f, 0.2439f, -0.0387f, -0.1953f, -0.3017f};
+        const bool km16 = p.model == EWF_MODEL_ISO_HET && p.vdamp != 0.0;
+        for (int q = 0; q < 6; ++q) mt[q] = km16 ? c16[q] : c9[q];
         xsrc = 180;
         zsrc = 200;
         stencil = 1;
@@ -243,7 +246,9 @@ extern "C" int ewf_load_legacy_inputs(ewf_handle *h)
         const int32_t r[16] = {504, 385, 1, EWF_F_VZ, 504, 385, 1, EWF_F_VX, 504, 388, 1, EWF_F_VY, 504, 387, 1, EWF_F_VY};
         memcpy(rec, r, sizeof(r));
     } else {
-        const int32_t r[16] = {631, 257, 1, EWF_F_VZ, 631, 257, 1, EWF_F_VX, 631, 257, 1, EWF_F_VY, 631, 257, 1, EWF_F_VY};
+        // ANISO:263-266 and 9kmst.cu: cell 631; the 16 km scheme: cell 981 (16kmst.cu:266-269)
+        const int32_t ix = (p.model == EWF_MODEL_ISO_HET && p.vdamp != 0.0) ? 981 : 631;
+        const int32_t r[16] = {ix, 257, 1, EWF_F_VZ, ix, 257, 1, EWF_F_VX, ix, 257, 1, EWF_F_VY, ix, 257, 1, EWF_F_VY};
         memcpy(rec, r, sizeof(r));
     }
     st = ewf_set_receivers(h, 4, rec);
