@@ -411,6 +411,20 @@ def main_batch(args):
                       "runs": runs, "cell_updates": cell_updates}}
     if clocks:
         out["clocks"] = clocks
+    # the reference's own kernels, one run at a time with their launch + synchronise pattern:
+    # each problem's per-run rate over a bounded sample of steps, summed over the runs
+    ref_s, rates = 0.0, []
+    for m, rl in probs:
+        r = reference_gpu(m, 100)
+        if r is None:
+            ref_s = None
+            break
+        rates.append(round(r["value"], 2))
+        ref_s += m.cells * nt * len(rl) / (r["value"] * 1e9)
+    if ref_s:
+        out["reference_kernels"] = {"runs_per_s": round(runs / ref_s, 4), "speedup_of_batch": round(ref_s / batch_s, 3),
+                                    "gcell_updates_per_s_per_problem": rates,
+                                    "what": "reference kernels (stock build), each run alone, 100-step samples"}
     print(json.dumps(out), flush=True)
 
 
