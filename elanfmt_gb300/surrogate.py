@@ -289,14 +289,16 @@ def geometry(m, src: np.ndarray, rec_xy: np.ndarray) -> np.ndarray:
     return np.stack([depth, off, az, np.hypot(off, depth)], axis=-1)
 
 
-def features(geo: np.ndarray, structured: bool) -> np.ndarray:
+def features(geo: np.ndarray, structured: bool, az4: bool = False) -> np.ndarray:
     """Network inputs.  structured: (depth, offset) -- the network predicts the fundamental traces,
-    which do not depend on azimuth.  Otherwise (depth, offset, cos az, sin az, cos 2az, sin 2az):
-    the radiation patterns of the elementary moment tensors are combinations of the first and
-    second azimuthal harmonics."""
+    which do not depend on azimuth in a laterally homogeneous medium; az4 adds cos 4az, sin 4az,
+    the lowest harmonic of a cubic grid's direction-dependent dispersion.  Otherwise (depth,
+    offset, cos az, sin az, cos 2az, sin 2az): the radiation patterns of the elementary moment
+    tensors are combinations of the first and second azimuthal harmonics."""
     depth, off, az = geo[..., 0], geo[..., 1], geo[..., 2]
     if structured:
-        return np.stack([depth, off], axis=-1).astype(np.float32)
+        cols = [depth, off] + ([np.cos(4 * az), np.sin(4 * az)] if az4 else [])
+        return np.stack(cols, axis=-1).astype(np.float32)
     return np.stack([depth, off, np.cos(az), np.sin(az), np.cos(2 * az), np.sin(2 * az)], axis=-1).astype(np.float32)
 
 
@@ -394,8 +396,21 @@ def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: i
                 Y=np.concatenate([t.reshape(len(t), -1) for t in traces]), fdtd_s_per_src=fdtd_s_per_src)
 
 
+def fourier_features(Xs: np.ndarray, sigma: float, width: int, seed: int = 0) -> np.ndarray:
+    """[Xs, sin(2 pi Xs B^T), cos(2 pi Xs B^T)] with B ~ N(0, sigma^2) (random Fourier features,
+    Tancik et al. 2020: an MLP fed with them fits oscillatory functions of its inputs far better),
+    `width` columns in all; sigma = 0 returns Xs."""
+    if sigma <= 0:
+        return Xs
+    nf = (width - Xs.shape[1]) // 2
+    B = np.random.default_rng(seed).normal(0.0, sigma, size=(nf, Xs.shape[1]))
+    proj = 2 * np.pi * Xs.astype(np.float64) @ B.T
+    return np.concatenate([Xs, np.sin(proj), np.cos(proj)], axis=1).astype(np.float32)
+
+
 def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 512, layers: int = 4,
-                     lr: float = 1e-3, spreading: bool = True, structured: bool = True, log=print) -> dict:
+                     lr: float = 1e-3, spreading: bool = True, structured: bool = True, fourier: float = 0.0,
+                     az4: bool = False, log=print) -> dict:
     """Trains the MLP on the training sources of a dataset and scores it on the held-out ones
     against the solver's traces; also scores the nearest-neighbour method (no network) and the
     fallback policy.  structured: the network maps (depth, offset) to the 10 fundamental traces
@@ -416,7 +431,7 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
     live = energy > 1e-3 * np.median(energy)
     test = ~is_train & live
     val_src = val_src & live
-    X = features(geo, structured)
+    X = features(geo, structured, az4)
     mu, sd = X[fit].mean(axis=0), X[fit].std(axis=0) + 1e-6
     Xs = (X - mu) / sd
     # geometric spreading: targets scaled by distance, so that near and far receivers weigh alike
@@ -434,12 +449,13 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
     nout = T.shape[1]
     fit_rows = np.nonzero(fit)[0]
     scale = float(np.sqrt(np.mean(T[fit_rows] ** 2)))
+    Xf_in = fourier_features(Xs, fourier, IN_PAD, seed)
     Xp = np.zeros((len(X), IN_PAD), np.float32)
-    Xp[:, :X.shape[1]] = Xs
+    Xp[:, :Xf_in.shape[1]] = Xf_in
     Xg = torch.from_numpy(Xp).cuda().to(torch.bfloat16)
     Tg = torch.from_numpy(T / scale).cuda()
     fit_idx = torch.from_numpy(fit_rows).cuda()
-    net = MLP([IN_PAD] + [hidden] * layers + [nout], seed=seed, fan_in0=X.shape[1])
+    net = MLP([IN_PAD] + [hidden] * layers + [nout], seed=seed, fan_in0=Xf_in.shape[1])
     t0 = time.perf_counter()
     losses = net.train(Xg.index_select(0, fit_idx), Tg.index_select(0, fit_idx), steps=steps, batch=256, lr=lr,
                        log_every=max(1, steps // 10))
@@ -521,6 +537,7 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
         "network": f"MLP {X.shape[1]}(->{IN_PAD} pad) -> {layers}x{hidden} GELU -> {nout}, bf16 weights, "
                    "fp32 accumulate",
         "structured": structured,
+        "fourier_sigma": fourier, "az4": az4,
         "features": ("depth, offset -> 10 fundamental traces, mixed per azimuth" if structured else
                      "depth, offset, cos/sin az, cos/sin 2az -> 18 traces") + " (standardised)" +
                     ("; targets x distance" if spreading else ""),
