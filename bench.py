@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--size", type=str, default="", help="override grid, e.g. 128x128x96 (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, cpu baseline, reference_gpu, kernel timing")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--step", default="split", choices=["split", "fused", "wave"],
+                    help="step form: two kernels (default), the one-pass kernel, or the wavefront launch")
+    ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
+    ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
     return ap.parse_args()
 
 
@@ -238,8 +242,12 @@ def main():
     torch.cuda.set_device(local)
     m, desc = workload(args.workload, args.nt, args.size)
     nt = m.nt
-    s = Solver.from_model(m)
-    kchunk = s.autotune(30)   # the library's z-chunk autotuner (resets the state)
+    form = {"split": F.STEP_SPLIT, "fused": F.STEP_FUSED, "wave": F.STEP_WAVE}[args.step]
+    s = Solver.from_model(m, fused=form, kchunk=args.kchunk)
+    # the library's autotuner (z-chunk; the wavefront lag too) unless both are given
+    kchunk = args.kchunk if args.kchunk and (form != F.STEP_WAVE or args.wave_lag) else s.autotune(30)
+    if form == F.STEP_WAVE and args.wave_lag:
+        s.set_wave(args.wave_lag)
 
     for _ in range(args.warmup):
         s.reset()
@@ -266,7 +274,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": nt, "receivers": len(m.receivers),
-                   "kchunk_autotuned": kchunk,
+                   "kchunk_autotuned": kchunk, "step": args.step,
+                   **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {}),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (working set ~%.1f GB)" % (m.cells * 4 * 21 / 1e9)},
         "gpu_launches": launches,
@@ -281,15 +290,20 @@ def main():
         # per-kernel CUDA-event timing on the solver's stream
         s.reset()
         kt = s.time_kernels(min(200, nt))
-        kb = KERNEL_BYTES[args.workload]
+        if form == F.STEP_SPLIT:
+            kb = KERNEL_BYTES[args.workload]
+            names = {"stress": "k_stress", "velocity": "k_velocity"}
+        else:  # one kernel does the whole step: its compulsory bytes are the one-pass step's
+            kb = {"stress": STEP_BYTES[args.workload]}
+            names = {"stress": "k_wave" if form == F.STEP_WAVE else "k_step"}
         kernels = {}
-        for k in ("stress", "velocity"):
+        for k in kb:
             achieved = kb[k] * m.cells / (kt[k] * 1e-3) / 1e9
             kernels[k] = {"ms": round(kt[k], 4), "bytes_per_cell": kb[k], "achieved_gbs": round(achieved, 1),
                           "frac": round(achieved / peak, 4)}
-        dom = max(("stress", "velocity"), key=lambda k: kt[k])
-        tr = ncu_traffic(f"k_{dom}", args.workload)
-        out["roofline"] = {"kernel": f"k_{dom}", "bound": "hbm", "achieved": kernels[dom]["achieved_gbs"],
+        dom = max(kb, key=lambda k: kt[k])
+        tr = ncu_traffic(names[dom], args.workload)
+        out["roofline"] = {"kernel": names[dom], "bound": "hbm", "achieved": kernels[dom]["achieved_gbs"],
                            "peak": peak, "unit": "GB/s", "frac": kernels[dom]["frac"],
                            "traffic": None if tr is None else round(tr * m.cells),
                            "algorithmic_bytes": kb[dom] * m.cells, "peak_kind": peak_kind}

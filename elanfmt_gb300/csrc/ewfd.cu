@@ -9,6 +9,7 @@
 #include "ewfd_internal.h"
 #include "ewfd_kernels.cuh"
 #include "ewfd_fused.cuh"
+#include "ewfd_wave.cuh"
 
 #include <cmath>
 #include <condition_variable>
@@ -179,6 +180,17 @@ struct ewf_handle {
     void *g_alloc[9] = {};  // second state buffer of the fused step
     bool fused = false;
     int flip = 0;           // fused: the current state is in g_alloc when 1
+    bool wave = false;      // wavefront step (ewfd_wave.cuh)
+    int nsm = 0;            // multiprocessors of the device
+    WaveCtl *d_wctl = nullptr;
+    int *d_wdone = nullptr;     // done flags, one per stress item
+    int wdone_cap = 0;
+    int *d_woff = nullptr;      // source entries grouped by owning stress item (n + 1 offsets)
+    SrcEntry *d_wsrc = nullptr;
+    int woff_cap = 0;
+    int wave_key[3] = {-1, -1, -1};  // (kslab, src_version, n) the grouping was built for
+    int src_version = 0;
+    int wave_lag_pct = 100;     // lag = ntx + 1 + CTAs * pct / 100 (autotuned)
     void *comp_alloc[3] = {};
     void *m_alloc[12] = {};
     bool m_set[12] = {};
@@ -433,6 +445,10 @@ extern "C" void ewf_destroy(ewf_handle *h)
     for (auto &x : h->w6_alloc) cudaFree(x);
     cudaFree(h->d_stf);
     cudaFree(h->d_src);
+    cudaFree(h->d_wctl);
+    cudaFree(h->d_wdone);
+    cudaFree(h->d_woff);
+    cudaFree(h->d_wsrc);
     cudaFree(h->d_rec_off);
     cudaFree(h->d_rec_comp);
     cudaFree(h->d_traces);
@@ -456,15 +472,16 @@ static int validate_params(const ewf_params *p)
     if (p->precision < EWF_PREC_F32 || p->precision > EWF_PREC_F64) return ewf_fail(EWF_ERR_ARG, "unknown precision %d", p->precision);
     if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D && p->damping != EWF_DAMP_PERCOMP)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles or per-component weights (damping 0 or 3)");
-    if (p->damping == EWF_DAMP_PERCOMP && (p->model != EWF_MODEL_ISO || p->fused))
-        return ewf_fail(EWF_ERR_UNSUPPORTED, "per-component weights: isotropic model, two-kernel step");
+    if (p->fused < EWF_STEP_SPLIT || p->fused > EWF_STEP_WAVE) return ewf_fail(EWF_ERR_ARG, "unknown step form %d", p->fused);
+    if (p->damping == EWF_DAMP_PERCOMP && (p->model != EWF_MODEL_ISO || p->fused == EWF_STEP_FUSED))
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "per-component weights: isotropic model, two-kernel or wavefront step");
     if (p->model != EWF_MODEL_ISO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the orthorhombic and 9 km schemes use a 3-D or separable weight field (damping 1 or 2)");
-    if (p->model == EWF_MODEL_ISO_HET && p->fused)
+    if (p->model == EWF_MODEL_ISO_HET && p->fused == EWF_STEP_FUSED)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the one-pass step is built for models 0 and 1");
     if (!(p->vdamp >= 0.0) || p->vdamp >= 1.0) return ewf_fail(EWF_ERR_ARG, "vdamp must be in [0, 1)");
-    if (p->vdamp != 0.0 && (p->model == EWF_MODEL_ISO || p->precision == EWF_PREC_F32_KAHAN || p->fused))
-        return ewf_fail(EWF_ERR_UNSUPPORTED, "vdamp applies to models 1 and 2 in FP32/FP64 with the two-kernel step");
+    if (p->vdamp != 0.0 && (p->model == EWF_MODEL_ISO || p->precision == EWF_PREC_F32_KAHAN || p->fused == EWF_STEP_FUSED))
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "vdamp applies to models 1 and 2 in FP32/FP64 with the two-kernel or wavefront step");
     if (p->src_order != EWF_SRC_BEFORE_BC1 && p->src_order != EWF_SRC_AFTER_BC1)
         return ewf_fail(EWF_ERR_ARG, "unknown src_order %d", p->src_order);
     if (p->over_y < 0) return ewf_fail(EWF_ERR_ARG, "over_y must be >= 0");
@@ -504,7 +521,7 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
     h->kchunk = p->kchunk > 0 ? p->kchunk : 16;
     h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
-    if (p->fused && (h->gsteps & 1)) h->gsteps += 1;  // fused graphs replay buffer pairs
+    if (p->fused == EWF_STEP_FUSED && (h->gsteps & 1)) h->gsteps += 1;  // fused graphs replay buffer pairs
 
 #define CKH(call)                                                                                    \
     do {                                                                                             \
@@ -525,7 +542,13 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     CKC(cudaEventCreate(&h->ev0));
     CKC(cudaEventCreate(&h->ev1));
-    h->fused = p->fused != 0;
+    h->fused = p->fused == EWF_STEP_FUSED;
+    h->wave = p->fused == EWF_STEP_WAVE;
+    CKC(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
+    if (h->wave) {
+        CKC(cudaMalloc(&h->d_wctl, sizeof(WaveCtl)));
+        CKC(cudaMemsetAsync(h->d_wctl, 0, sizeof(WaveCtl), h->stream));
+    }
     if (p->model == EWF_MODEL_ORTHO && h->esz == 4)
         h->fdiv = ewf_fdiv_verified((float)p->dx) && ewf_fdiv_verified((float)p->dy) && ewf_fdiv_verified((float)p->dz);
     for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
@@ -791,6 +814,7 @@ extern "C" int ewf_set_sources(ewf_handle *h, int32_t n, const int32_t *cijk, co
     if (n > 0) CK(cudaMemcpy(h->d_src, v.data(), (size_t)n * sizeof(SrcEntry), cudaMemcpyHostToDevice));
     h->h_src = v;
     h->nsrc = n;
+    h->src_version++;
     h->graph_dirty = true;
     return EWF_OK;
 }
@@ -881,6 +905,10 @@ extern "C" int ewf_reset(ewf_handle *h)
     for (auto x : h->comp_alloc) { int s = dev_zero(h, x); if (s) return s; }
     if (h->d_traces) CK(cudaMemsetAsync(h->d_traces, 0, (size_t)h->nrec * h->p.nt * sizeof(double), h->stream));
     CK(cudaMemsetAsync(h->d_it, 0, sizeof(int), h->stream));
+    if (h->d_wctl) {  // ticket and error flag; the generation keeps counting (stale done flags stay below it)
+        CK(cudaMemsetAsync(&h->d_wctl->ticket, 0, sizeof(int), h->stream));
+        CK(cudaMemsetAsync(&h->d_wctl->err, 0, sizeof(int), h->stream));
+    }
     CK(cudaStreamSynchronize(h->stream));
     h->it = 0;
     return EWF_OK;
@@ -943,48 +971,157 @@ static void fused_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
-template <bool FUSED, typename T, int MODEL, int DAMP, bool KAHAN>
-static step_fn entry()
+// The wavefront step: shape, done flags and the per-item grouping of the point sources for the
+// current z-chunk (rebuilt when the chunk or the sources change; never during graph capture).
+static WaveShape wave_shape_of(const ewf_handle *h, int lag)
 {
-    return FUSED ? fused_entry<T, MODEL, DAMP, KAHAN> : step_entry<T, MODEL, DAMP, KAHAN>;
+    return wave_shape(h->p.nx, h->p.ny, h->p.nz, TX, TY, h->kchunk, lag);
 }
 
-template <bool FUSED>
+static int wave_prepare(ewf_handle *h)
+{
+    if (!h->wave) return EWF_OK;
+    const WaveShape w = wave_shape_of(h, 0);
+    if (h->wave_key[0] == w.kslab && h->wave_key[1] == h->src_version && h->wave_key[2] == w.n) return EWF_OK;
+    CK(cudaStreamSynchronize(h->stream));
+    if (w.n > h->wdone_cap) {
+        cudaFree(h->d_wdone);
+        h->d_wdone = nullptr;
+        h->wdone_cap = 0;
+        CK(cudaMalloc(&h->d_wdone, (size_t)w.n * sizeof(int)));
+        CK(cudaMemset(h->d_wdone, 0, (size_t)w.n * sizeof(int)));  // below every generation + 1
+        h->wdone_cap = w.n;
+    }
+    // stable grouping by owner: entries of one item keep their order (k_inject's sum order)
+    std::vector<int> off((size_t)w.n + 1, 0);
+    std::vector<int> owner(h->h_src.size());
+    for (size_t e = 0; e < h->h_src.size(); ++e) {
+        const SrcEntry &q = h->h_src[e];
+        owner[e] = wave_owner(w, TX, TY, q.i, q.j, q.k);
+        off[(size_t)owner[e] + 1]++;
+    }
+    for (int i = 0; i < w.n; ++i) off[(size_t)i + 1] += off[(size_t)i];
+    std::vector<SrcEntry> grouped(h->h_src.size());
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (size_t e = 0; e < h->h_src.size(); ++e) grouped[(size_t)fill[(size_t)owner[e]]++] = h->h_src[e];
+    if (w.n + 1 > h->woff_cap) {
+        cudaFree(h->d_woff);
+        cudaFree(h->d_wsrc);
+        h->d_woff = nullptr;
+        h->d_wsrc = nullptr;
+        h->woff_cap = 0;
+        CK(cudaMalloc(&h->d_woff, (size_t)(w.n + 1) * sizeof(int)));
+        CK(cudaMalloc(&h->d_wsrc, (size_t)MAXSRC * sizeof(SrcEntry)));
+        h->woff_cap = w.n + 1;
+    }
+    CK(cudaMemcpy(h->d_woff, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!grouped.empty())
+        CK(cudaMemcpy(h->d_wsrc, grouped.data(), grouped.size() * sizeof(SrcEntry), cudaMemcpyHostToDevice));
+    h->wave_key[0] = w.kslab;
+    h->wave_key[1] = h->src_version;
+    h->wave_key[2] = w.n;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+// reads and clears the wavefront step's error flag (after the stream has been synchronised)
+static int wave_check(ewf_handle *h)
+{
+    if (!h->wave) return EWF_OK;
+    WaveCtl c;
+    CK(cudaMemcpy(&c, h->d_wctl, sizeof(c), cudaMemcpyDeviceToHost));
+    if (c.err) {
+        CK(cudaMemset(&h->d_wctl->err, 0, sizeof(int)));
+        return ewf_fail(EWF_ERR_CUDA, "wavefront step: a dependency wait gave up; the state of this run is invalid");
+    }
+    return EWF_OK;
+}
+
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+static void wave_entry(const ewf_handle *h, cudaEvent_t *ev, int)
+{
+    const StepArgs<T> a = make_args<T>(h, 0);
+    constexpr int MB = sizeof(T) == 4 ? 3 : 1;
+    auto kern = k_wave<T, MODEL, DAMP, KAHAN, MB>;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WAVE_THREADS, 0);
+    const WaveShape w0 = wave_shape_of(h, 0);
+    int ctas = std::max(1, per_sm) * std::max(1, h->nsm);
+    ctas = std::min(ctas, 2 * w0.n);
+    WaveArgs wa;
+    memset(&wa, 0, sizeof(wa));
+    wa.w = wave_shape_of(h, w0.ntx + 1 + (int)((long long)ctas * h->wave_lag_pct / 100));
+    wa.ctl = h->d_wctl;
+    wa.done = h->d_wdone;
+    wa.src_off = h->d_woff;
+    wa.src = h->d_wsrc;
+    wa.stf = h->d_stf;
+    wa.nstf = (int)h->nstf;
+    wa.it_ptr = h->d_it;
+    wa.order = h->p.src_order;
+    if (ev) cudaEventRecord(ev[0], h->stream);
+    kern<<<ctas, WAVE_THREADS, 0, h->stream>>>(a, wa);
+    if (ev) {
+        cudaEventRecord(ev[1], h->stream);
+        cudaEventRecord(ev[2], h->stream);
+        cudaEventRecord(ev[3], h->stream);
+    }
+    k_record<T><<<1, 256, 0, h->stream>>>(a, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    if (ev) cudaEventRecord(ev[4], h->stream);
+}
+
+template <int FORM, typename T, int MODEL, int DAMP, bool KAHAN>
+static step_fn entry()
+{
+    if (FORM == EWF_STEP_FUSED) return fused_entry<T, MODEL, DAMP, KAHAN>;
+    if (FORM == EWF_STEP_WAVE) return wave_entry<T, MODEL, DAMP, KAHAN>;
+    return step_entry<T, MODEL, DAMP, KAHAN>;
+}
+
+// FORM: EWF_STEP_*; the one-pass form exists for models 0 and 1 with 1-D, 3-D or separable
+// damping (validated), the others for every combination
+template <int FORM>
 static step_fn pick_step_t(const ewf_params &p)
 {
+    constexpr int F2 = FORM == EWF_STEP_FUSED ? EWF_STEP_SPLIT : FORM;  // forms built for every model
     const bool iso = p.model == EWF_MODEL_ISO;
     const bool w3 = p.damping == EWF_DAMP_W3D;
-    if (p.damping == EWF_DAMP_PERCOMP) {  // isotropic, two-kernel step only (validated)
+    if (p.damping == EWF_DAMP_PERCOMP) {
         switch (p.precision) {
-        case EWF_PREC_F32: return step_entry<float, MODEL_ISO, DAMP_PERCOMP, false>;
-        case EWF_PREC_F32_KAHAN: return step_entry<float, MODEL_ISO, DAMP_PERCOMP, true>;
-        default: return step_entry<double, MODEL_ISO, DAMP_PERCOMP, false>;
+        case EWF_PREC_F32: return entry<F2, float, MODEL_ISO, DAMP_PERCOMP, false>();
+        case EWF_PREC_F32_KAHAN: return entry<F2, float, MODEL_ISO, DAMP_PERCOMP, true>();
+        default: return entry<F2, double, MODEL_ISO, DAMP_PERCOMP, false>();
         }
     }
-    if (p.model == EWF_MODEL_ISO_HET) {  // two-kernel step only (validated)
+    if (p.model == EWF_MODEL_ISO_HET) {
         switch (p.precision) {
         case EWF_PREC_F32:
-            return w3 ? step_entry<float, MODEL_ISOHET, DAMP_W3D, false> : step_entry<float, MODEL_ISOHET, DAMP_SEP, false>;
+            return w3 ? entry<F2, float, MODEL_ISOHET, DAMP_W3D, false>() : entry<F2, float, MODEL_ISOHET, DAMP_SEP, false>();
         case EWF_PREC_F32_KAHAN:
-            return w3 ? step_entry<float, MODEL_ISOHET, DAMP_W3D, true> : step_entry<float, MODEL_ISOHET, DAMP_SEP, true>;
+            return w3 ? entry<F2, float, MODEL_ISOHET, DAMP_W3D, true>() : entry<F2, float, MODEL_ISOHET, DAMP_SEP, true>();
         default:
-            return w3 ? step_entry<double, MODEL_ISOHET, DAMP_W3D, false> : step_entry<double, MODEL_ISOHET, DAMP_SEP, false>;
+            return w3 ? entry<F2, double, MODEL_ISOHET, DAMP_W3D, false>() : entry<F2, double, MODEL_ISOHET, DAMP_SEP, false>();
         }
     }
     switch (p.precision) {
     case EWF_PREC_F32:
-        if (iso) return entry<FUSED, float, MODEL_ISO, DAMP_PML1D, false>();
-        return w3 ? entry<FUSED, float, MODEL_ORTHO, DAMP_W3D, false>() : entry<FUSED, float, MODEL_ORTHO, DAMP_SEP, false>();
+        if (iso) return entry<FORM, float, MODEL_ISO, DAMP_PML1D, false>();
+        return w3 ? entry<FORM, float, MODEL_ORTHO, DAMP_W3D, false>() : entry<FORM, float, MODEL_ORTHO, DAMP_SEP, false>();
     case EWF_PREC_F32_KAHAN:
-        if (iso) return entry<FUSED, float, MODEL_ISO, DAMP_PML1D, true>();
-        return w3 ? entry<FUSED, float, MODEL_ORTHO, DAMP_W3D, true>() : entry<FUSED, float, MODEL_ORTHO, DAMP_SEP, true>();
+        if (iso) return entry<FORM, float, MODEL_ISO, DAMP_PML1D, true>();
+        return w3 ? entry<FORM, float, MODEL_ORTHO, DAMP_W3D, true>() : entry<FORM, float, MODEL_ORTHO, DAMP_SEP, true>();
     default:
-        if (iso) return entry<FUSED, double, MODEL_ISO, DAMP_PML1D, false>();
-        return w3 ? entry<FUSED, double, MODEL_ORTHO, DAMP_W3D, false>() : entry<FUSED, double, MODEL_ORTHO, DAMP_SEP, false>();
+        if (iso) return entry<FORM, double, MODEL_ISO, DAMP_PML1D, false>();
+        return w3 ? entry<FORM, double, MODEL_ORTHO, DAMP_W3D, false>() : entry<FORM, double, MODEL_ORTHO, DAMP_SEP, false>();
     }
 }
 
-static step_fn pick_step(const ewf_handle *h) { return h->fused ? pick_step_t<true>(h->p) : pick_step_t<false>(h->p); }
+static step_fn pick_step(const ewf_handle *h)
+{
+    if (h->fused) return pick_step_t<EWF_STEP_FUSED>(h->p);
+    if (h->wave) return pick_step_t<EWF_STEP_WAVE>(h->p);
+    return pick_step_t<EWF_STEP_SPLIT>(h->p);
+}
 
 static int inputs_ready(const ewf_handle *h)
 {
@@ -1038,6 +1175,7 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
         return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
     if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf)
         return ewf_fail(EWF_ERR_ARG, "source time function has %zu samples, need %d", h->nstf, h->it + nsteps);
+    if ((st = wave_prepare(h))) return st;
     const step_fn fn = pick_step(h);
     const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + (h->fused ? h->flip : 0);
     if (use_graph && (h->graph_dirty || !h->gexec)) {
@@ -1071,6 +1209,7 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     h->it += nsteps;
+    if ((st = wave_check(h))) return st;
     if (h->p.check_finite && h->nrec > 0 && nsteps > 0) {
         // only the samples of this call: columns [it - nsteps, it) of the nrec x nt traces
         const int t0 = h->it - nsteps;
@@ -1092,6 +1231,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     if (st) return st;
     if (h->it + nsteps > h->p.nt) return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
     if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf) return ewf_fail(EWF_ERR_ARG, "source time function too short");
+    if ((st = wave_prepare(h))) return st;
     const step_fn fn = pick_step(h);
     cudaEvent_t ev[5] = {};
     for (auto &e : ev) CK(cudaEventCreate(&e));
@@ -1111,6 +1251,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     if (err) return err;
     CK(cudaGetLastError());
     h->it += nsteps;
+    if ((st = wave_check(h))) return st;
     for (int q = 0; q < 4; ++q) out_ms[q] = acc[q] / nsteps;
     return EWF_OK;
 }
@@ -1125,35 +1266,70 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     if (steps < 1) return ewf_fail(EWF_ERR_ARG, "nt too small to tune");
     if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
     float best = 1e30f;
-    int best_k = h->kchunk;
+    int best_k = h->kchunk, best_lag = h->wave_lag_pct;
+    // wavefront step: slabs of 4..16 planes x lag (100000: every stress item before the first velocity item)
+    static const int lag_pct[] = {50, 100, 200, 100000};
+    const int nvar = h->wave ? 4 : 1;
     for (int kc : cand) {
         if (kc > h->p.nz && kc != cand[0]) continue;
-        h->kchunk = std::max(4, std::min(kc, h->p.nz));
-        if ((st = ewf_reset(h))) return st;
-        const step_fn fn = pick_step(h);
-        fn(h, nullptr, h->flip);  // warm
-        if (h->fused) h->flip ^= 1;
-        CK(cudaEventRecord(h->ev0, h->stream));
-        for (int s = 0; s < steps; ++s) {
-            fn(h, nullptr, h->flip);
+        if (h->wave && kc > 16) continue;
+        for (int vi = 0; vi < nvar; ++vi) {
+            h->kchunk = std::max(4, std::min(kc, h->p.nz));
+            if (h->wave) {
+                h->wave_lag_pct = lag_pct[vi];
+                h->graph_dirty = true;
+            }
+            if ((st = ewf_reset(h))) return st;
+            if ((st = wave_prepare(h))) return st;
+            const step_fn fn = pick_step(h);
+            fn(h, nullptr, h->flip);  // warm
             if (h->fused) h->flip ^= 1;
+            CK(cudaEventRecord(h->ev0, h->stream));
+            for (int s = 0; s < steps; ++s) {
+                fn(h, nullptr, h->flip);
+                if (h->fused) h->flip ^= 1;
+            }
+            CK(cudaEventRecord(h->ev1, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if ((st = wave_check(h))) return st;
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+            if (ms < best) {
+                best = ms;
+                best_k = h->kchunk;
+                best_lag = h->wave_lag_pct;
+            }
         }
-        CK(cudaEventRecord(h->ev1, h->stream));
-        CK(cudaStreamSynchronize(h->stream));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-        if (ms < best) { best = ms; best_k = h->kchunk; }
     }
     h->kchunk = best_k;
+    h->wave_lag_pct = best_lag;
     h->graph_dirty = true;
     if (kchunk) *kchunk = best_k;
     return ewf_reset(h);
 }
 
+extern "C" int ewf_set_wave(ewf_handle *h, int32_t lag_pct)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (!h->wave) return ewf_fail(EWF_ERR_STATE, "not a wavefront-step handle");
+    if (lag_pct < 1 || lag_pct > 100000) return ewf_fail(EWF_ERR_ARG, "lag_pct must be in [1, 100000] (got %d)", lag_pct);
+    h->wave_lag_pct = lag_pct;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct)
+{
+    if (!h || !lag_pct) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    if (!h->wave) return ewf_fail(EWF_ERR_STATE, "not a wavefront-step handle");
+    *lag_pct = h->wave_lag_pct;
+    return EWF_OK;
+}
+
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
 {
     if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *n = h->fused ? 2 : 3 + (h->nsrc > 0 ? 1 : 0);
+    *n = (h->fused || h->wave) ? 2 : 3 + (h->nsrc > 0 ? 1 : 0);
     return EWF_OK;
 }
 

@@ -63,6 +63,16 @@ struct SrcEntry {
 template <typename T>
 __device__ __forceinline__ T ld(const T *p) { return __ldg(p); }
 
+// State loads.  COH = false: the read-only path (the field is not written during the launch).
+// COH = true: a plain coherent load, for the wavefront step, where other CTAs of the same
+// launch write the fields (ordered by its release/acquire flags).
+template <bool COH, typename T>
+__device__ __forceinline__ T lds(const T *p)
+{
+    if constexpr (COH) return *p;
+    else return __ldg(p);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Division by a grid spacing.  The orthorhombic shear terms divide velocity differences by dx,
 // dy, dz (ANISO:327-352), and six IEEE divisions per cell cost a sixth of the stress kernel's
@@ -107,22 +117,22 @@ struct StressIn {
 };
 
 // c: state index (x stride R), cm: material index of the same cell
-template <typename T, int MODEL, int DAMP, int RC>
+template <typename T, int MODEL, int DAMP, int RC, bool COH = false>
 __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k,
                                             StressIn<T, MODEL, DAMP> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
     const long long sy = (RC == 1) ? a.sy : a.sys;
-    q.vx = ld(a.f[0] + c);
-    q.vx_ip = ld(a.f[0] + c + R);
-    q.vx_jm = ld(a.f[0] + c - sx);
-    q.vy = ld(a.f[1] + c);
-    q.vy_jp = ld(a.f[1] + c + sx);
-    q.vy_im = ld(a.f[1] + c - R);
-    q.vz_p = ld(a.f[2] + c + sy);
-    q.vz_im = ld(a.f[2] + c - R);
-    q.vz_jm = ld(a.f[2] + c - sx);
+    q.vx = lds<COH>(a.f[0] + c);
+    q.vx_ip = lds<COH>(a.f[0] + c + R);
+    q.vx_jm = lds<COH>(a.f[0] + c - sx);
+    q.vy = lds<COH>(a.f[1] + c);
+    q.vy_jp = lds<COH>(a.f[1] + c + sx);
+    q.vy_im = lds<COH>(a.f[1] + c - R);
+    q.vz_p = lds<COH>(a.f[2] + c + sy);
+    q.vz_im = lds<COH>(a.f[2] + c - R);
+    q.vz_jm = lds<COH>(a.f[2] + c - sx);
 #pragma unroll
     for (int f = 0; f < 6; ++f) q.s[f] = a.f[3 + f][c];
     if (MODEL == MODEL_ISO) {
@@ -150,8 +160,8 @@ __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, l
 // The column (X = i*R + r, j) over planes [k0, k1): X runs over the cells of every RHS.
 // RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
 // SOFF (with RC = 1): the state lives soff elements after the materials' index (one of several
-// right-hand sides in separate boxes of the same geometry).
-template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false>
+// right-hand sides in separate boxes of the same geometry).  COH: coherent state loads (lds).
+template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false, bool COH = false>
 __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1, long long soff = 0)
 {
     constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices
@@ -176,18 +186,18 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
 
     long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys + (SOFF ? soff : 0);
     long long cm = !SEP ? c : (RC == 1) ? c - soff : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
-    T vx_m = ld(a.f[0] + c - sys);  // Vx(k-1)
-    T vy_m = ld(a.f[1] + c - sys);  // Vy(k-1)
-    T vz_k = ld(a.f[2] + c);        // Vz(k)
+    T vx_m = lds<COH>(a.f[0] + c - sys);  // Vx(k-1)
+    T vy_m = lds<COH>(a.f[1] + c - sys);  // Vy(k-1)
+    T vz_k = lds<COH>(a.f[2] + c);        // Vz(k)
     T wz_k = T(0);
     if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + k0);
     StressIn<T, MODEL, DAMP> nxt;
-    stress_load<T, MODEL, DAMP, RC>(a, c, SEP ? cm : c, k0, nxt);
+    stress_load<T, MODEL, DAMP, RC, COH>(a, c, SEP ? cm : c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sys) {
         if (SEP && k > k0) cm += sy;
         const StressIn<T, MODEL, DAMP> q = nxt;
-        if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
+        if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC, COH>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
         const T Vxx = (q.vx_ip - q.vx) * rdx;
         const T Vyy = (q.vy_jp - q.vy) * rdy;
         const T Vzz = (q.vz_p - vz_k) * rdz;
@@ -285,6 +295,23 @@ __global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 4 : 1) k_stress(cons
 // refreshes the copy.  order 1 is "BC1, then inject" (ANISO:533-535).
 // ---------------------------------------------------------------------------------------------
 template <typename T>
+__device__ __forceinline__ void inject_entry(const StepArgs<T> &a, const SrcEntry &q, T s, int order)
+{
+    const long long c = (long long)q.i * a.R + (long long)q.j * a.sxs + (long long)q.k * a.sys;
+    T *f = a.f[q.comp];
+    if (order == 0) {
+        const bool row_bc = q.j < a.bc1_rows;
+        const bool xz_bc = (q.comp == 7) && q.i > 0 && q.i < a.nx && row_bc;
+        const bool yz_bc = (q.comp == 8) && q.j > 0 && q.j < a.ny && q.i < a.nx;
+        if ((q.comp == 5 && q.k == 0 && row_bc) || ((xz_bc || yz_bc) && q.k == 1)) return;
+        f[c] = f[c] + (T)q.coef * s;
+        if ((xz_bc || yz_bc) && q.k == 2) f[c - a.sys] = a.third * f[c];
+    } else {
+        f[c] = f[c] + (T)q.coef * s;
+    }
+}
+
+template <typename T>
 __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, int nsrc,
                          const double *__restrict__ stf, int nstf, const int *__restrict__ it_ptr, int order)
 {
@@ -292,21 +319,7 @@ __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, 
     const int it = *it_ptr;
     if (it < 0 || it >= nstf) return;  // the host validates the step range; never read past Src
     const T s = (T)stf[it];
-    for (int e = 0; e < nsrc; ++e) {
-        const SrcEntry q = src[e];
-        const long long c = (long long)q.i * a.R + (long long)q.j * a.sxs + (long long)q.k * a.sys;
-        T *f = a.f[q.comp];
-        if (order == 0) {
-            const bool row_bc = q.j < a.bc1_rows;
-            const bool xz_bc = (q.comp == 7) && q.i > 0 && q.i < a.nx && row_bc;
-            const bool yz_bc = (q.comp == 8) && q.j > 0 && q.j < a.ny && q.i < a.nx;
-            if ((q.comp == 5 && q.k == 0 && row_bc) || ((xz_bc || yz_bc) && q.k == 1)) continue;
-            f[c] = f[c] + (T)q.coef * s;
-            if ((xz_bc || yz_bc) && q.k == 2) f[c - a.sys] = a.third * f[c];
-        } else {
-            f[c] = f[c] + (T)q.coef * s;
-        }
-    }
+    for (int e = 0; e < nsrc; ++e) inject_entry(a, src[e], s, order);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -326,25 +339,25 @@ struct VelIn {
     T cp[KAHAN ? 3 : 1];
 };
 
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC>
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool COH = false>
 __device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k,
                                          VelIn<T, MODEL, DAMP, KAHAN> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
     const long long sy = (RC == 1) ? a.sy : a.sys;
-    q.sxx = ld(a.f[3] + c);
-    q.sxx_im = ld(a.f[3] + c - R);
-    q.syy = ld(a.f[4] + c);
-    q.syy_jm = ld(a.f[4] + c - sx);
-    q.szz = ld(a.f[5] + c);
-    q.sxy = ld(a.f[6] + c);
-    q.sxy_jp = ld(a.f[6] + c + sx);
-    q.sxy_ip = ld(a.f[6] + c + R);
-    q.sxz_p = ld(a.f[7] + c + sy);
-    q.sxz_ip = ld(a.f[7] + c + R);
-    q.syz_p = ld(a.f[8] + c + sy);
-    q.syz_jp = ld(a.f[8] + c + sx);
+    q.sxx = lds<COH>(a.f[3] + c);
+    q.sxx_im = lds<COH>(a.f[3] + c - R);
+    q.syy = lds<COH>(a.f[4] + c);
+    q.syy_jm = lds<COH>(a.f[4] + c - sx);
+    q.szz = lds<COH>(a.f[5] + c);
+    q.sxy = lds<COH>(a.f[6] + c);
+    q.sxy_jp = lds<COH>(a.f[6] + c + sx);
+    q.sxy_ip = lds<COH>(a.f[6] + c + R);
+    q.sxz_p = lds<COH>(a.f[7] + c + sy);
+    q.sxz_ip = lds<COH>(a.f[7] + c + R);
+    q.syz_p = lds<COH>(a.f[8] + c + sy);
+    q.syz_jp = lds<COH>(a.f[8] + c + sx);
 #pragma unroll
     for (int f = 0; f < 3; ++f) q.v[f] = a.f[f][c];
     if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
@@ -380,7 +393,7 @@ __device__ __forceinline__ T vel_update(const StepArgs<T> &a, T V, T dS, T w_or_
     return t;
 }
 
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false>
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, bool COH = false>
 __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0)
 {
     constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices (see stress_column)
@@ -409,16 +422,16 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
 
     long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys + (SOFF ? soff : 0);
     long long cm = !SEP ? c : (RC == 1) ? c - soff : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
-    T szz_m = ld(a.f[5] + c - sys);
-    T sxz_k = ld(a.f[7] + c);
-    T syz_k = ld(a.f[8] + c);
+    T szz_m = lds<COH>(a.f[5] + c - sys);
+    T sxz_k = lds<COH>(a.f[7] + c);
+    T syz_k = lds<COH>(a.f[8] + c);
     VelIn<T, MODEL, DAMP, KAHAN> nxt;
-    vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c, SEP ? cm : c, k0, nxt);
+    vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c, SEP ? cm : c, k0, nxt);
 
     for (int k = k0; k < k1; ++k, c += sys) {
         if (SEP && k > k0) cm += sy;
         VelIn<T, MODEL, DAMP, KAHAN> q = nxt;
-        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
+        if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
         const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
         const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
         const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;

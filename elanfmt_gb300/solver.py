@@ -73,6 +73,8 @@ SIGNATURES = {
     "ewf_pack_field_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int64, C.c_void_p, C.c_int32,
                                          C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_batch_create": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ewf_batch_destroy": (None, [C.c_void_p]),
     "ewf_batch_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t, C.c_int32]),
@@ -154,7 +156,8 @@ class Solver:
     @classmethod
     def from_model(cls, m, precision: int = F.PREC_F32, kchunk: int = 0, graph_steps: int = 0,
                    check_finite: bool = True, damping: int | None = None, nout: int = 0,
-                   fused: bool | None = None, workdir: str | None = None) -> "Solver":
+                   fused: int | None = None, workdir: str | None = None) -> "Solver":
+        """`fused`: the step form, F.STEP_SPLIT (default), F.STEP_FUSED or F.STEP_WAVE."""
         p = default_params()
         p.nx, p.ny, p.nz, p.nt = m.nx, m.ny, m.nz, m.nt
         p.model, p.precision = m.model, precision
@@ -269,6 +272,16 @@ class Solver:
         k = C.c_int32()
         _check(self._lib.ewf_autotune(self._h, int(nsteps), C.byref(k)), "ewf_autotune")
         return k.value
+
+    def set_wave(self, lag_pct: int) -> None:
+        """Wavefront step: lag of the velocity items behind the stress items, percent of the resident
+        CTAs (the autotuner sets it; results do not depend on it)."""
+        _check(self._lib.ewf_set_wave(self._h, int(lag_pct)), "ewf_set_wave")
+
+    def wave_lag(self) -> int:
+        lag = C.c_int32()
+        _check(self._lib.ewf_get_wave(self._h, C.byref(lag)), "ewf_get_wave")
+        return lag.value
 
     def launches_per_step(self) -> int:
         n = C.c_int32()

@@ -68,6 +68,14 @@ typedef enum ewf_damping {
                              * FastWaveED_GPU3D_v1.cu:298-320, 344-360), ANISO's loop order */
 } ewf_damping;
 
+typedef enum ewf_step_form {
+    EWF_STEP_SPLIT = 0, /* stress kernel, injection, velocity kernel (reference order OK4:485-498) */
+    EWF_STEP_FUSED = 1, /* one-pass step kernel, double-buffered state (models 0 and 1) */
+    EWF_STEP_WAVE = 2   /* one persistent launch of the stress and velocity updates over tile x slab
+                         * items in dependency order, in place: the velocity update reads the new
+                         * stresses back from L2 (every model, damping and precision) */
+} ewf_step_form;
+
 typedef enum ewf_src_order {
     EWF_SRC_BEFORE_BC1 = 0, /* OK4: injection inside the stress kernel, BC1 after (OK4:336-342, 490) */
     EWF_SRC_AFTER_BC1 = 1   /* ANISO: BC1, then the source kernel (ANISO:533-535) */
@@ -108,14 +116,14 @@ typedef struct ewf_params {
     int32_t kchunk;       /* planes per CTA of the z-marching kernels; 0 = autotuned/default */
     int32_t graph_steps;  /* steps captured per CUDA graph; 0 = default, <0 = no graph */
     int32_t check_finite; /* 1: ewf_run checks the receiver traces for NaN/Inf */
-    int32_t fused;        /* 0 (default): stress and velocity kernels; 1: one-pass step kernel (double-buffered state) */
+    int32_t fused;        /* ewf_step_form: 0 (default) two kernels; 1 one-pass kernel; 2 wavefront */
     double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
     double c66;            /* isotropic shear modulus pa2[7] (OK4:405); PERCOMP: the xy one */
     double c44, c55;       /* PERCOMP shear moduli of yz and xz, pa2[5], pa2[6] */
     double bx, by, bz;     /* isotropic 1/rho pa3[0..2] (OK4:407) */
     double vdamp;          /* linear velocity damping: V_new = update - vdamp * V_old (16 km station
                             * scheme, FastWaveED_GPU3D_v1_16kmst.cu:337-349, vdamp = 2.2 * 4.6729e-04
-                            * in float); 0 = off.  Models 1 and 2, FP32 / FP64, two-kernel step. */
+                            * in float); 0 = off.  Models 1 and 2, FP32 / FP64, not the one-pass step. */
     const char *workdir;   /* legacy *.dat inputs and *.res outputs (NULL = ".") */
 } ewf_params;
 
@@ -178,15 +186,22 @@ int ewf_last_run_ms(const ewf_handle *h, double *ms);
 
 /* Diagnostics: advances nsteps time steps launching each kernel between CUDA events on the
  * handle's stream (no graph) and returns the average device time per launch in ms of
- * out_ms[0] stress (the whole fused step when fused), [1] injection, [2] velocity, [3] receiver
+ * out_ms[0] stress (the whole step for the one-pass and wavefront forms), [1] injection, [2] velocity, [3] receiver
  * gather (0 for kernels the step does not launch). */
 int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4]);
 /* Number of kernel launches one time step issues. */
 int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
 
 /* Autotuner: times `nsteps` steps for each z-chunk candidate (planes per CTA) with CUDA events,
- * keeps the fastest (returned in *kchunk, may be NULL) and resets the state. */
+ * keeps the fastest (returned in *kchunk, may be NULL) and resets the state.  The wavefront
+ * step also tunes its lag (kept in the handle). */
 int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
+
+/* Wavefront step (fused = EWF_STEP_WAVE): the lag of the velocity items behind the stress items
+ * in percent of the resident CTAs, 1..100000 (set by ewf_autotune; results do not depend on it).
+ * EWF_ERR_STATE for the other step forms. */
+int ewf_set_wave(ewf_handle *h, int32_t lag_pct);
+int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct);
 
 /* Writes 0_infos.inf and 0_0_{Src,Rec,Rec_x,Rec_y,Rec_y2,Vx,Vy,Vz}.res into workdir
  * (OK4:521-532).  Rec* are the first four receivers. */

@@ -49,7 +49,9 @@ CASES = [
 ]
 
 
-FUSED = pytest.mark.parametrize("fused", [True, False], ids=["fused", "split"])
+FUSED = pytest.mark.parametrize("fused", [F.STEP_FUSED, F.STEP_SPLIT, F.STEP_WAVE], ids=["fused", "split", "wave"])
+# step forms built for every model and damping
+FORMS = pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_WAVE], ids=["split", "wave"])
 
 
 @pytest.mark.parametrize("name,model,damping,nx,ny,nz", CASES, ids=[c[0] for c in CASES])
@@ -69,30 +71,33 @@ ISOHET_CASES = [
 
 @pytest.mark.parametrize("name,damping,nx,ny,nz", ISOHET_CASES, ids=[c[0] for c in ISOHET_CASES])
 @pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
-def test_isohet_bitwise_vs_oracle(cuda_device, name, damping, nx, ny, nz, prec):
-    """The 9 km scheme (edge shear moduli, staggered buoyancy; two-kernel step only)."""
+@FORMS
+def test_isohet_bitwise_vs_oracle(cuda_device, name, damping, nx, ny, nz, prec, form):
+    """The 9 km scheme (edge shear moduli, staggered buoyancy; not the one-pass step)."""
     m = I.random_small(F.MODEL_ISO_HET, nx, ny, nz, nt=48, seed=nx * 5 + nz, damping=damping)
     ref = O.run(m, 48, prec)
-    assert_bitwise(product(m, 48, prec), ref, name)
+    assert_bitwise(product(m, 48, prec, fused=form), ref, name)
 
 
 @pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
 @pytest.mark.parametrize("nx,ny,nz", [(35, 40, 21), (29, 30, 27)])
-def test_percomp_bitwise_vs_oracle(cuda_device, prec, nx, ny, nz):
+@FORMS
+def test_percomp_bitwise_vs_oracle(cuda_device, prec, nx, ny, nz, form):
     """The DC_Earthquake form: isotropic, one 3-D weight field per component, three shear moduli."""
     m = I.random_small(F.MODEL_ISO, nx, ny, nz, nt=48, seed=nx + 3 * nz, damping=F.DAMP_PERCOMP)
     ref = O.run(m, 48, prec)
-    assert_bitwise(product(m, 48, prec), ref, "percomp")
+    assert_bitwise(product(m, 48, prec, fused=form), ref, "percomp")
 
 
 @pytest.mark.parametrize("model", [F.MODEL_ORTHO, F.MODEL_ISO_HET], ids=["ortho", "isohet"])
 @pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F64], ids=["f32", "f64"])
-def test_velocity_damping_bitwise_vs_oracle(cuda_device, model, prec):
+@FORMS
+def test_velocity_damping_bitwise_vs_oracle(cuda_device, model, prec, form):
     """Linear velocity damping of the 16 km scheme (V -= vdamp * V_old after each update)."""
     m = I.random_small(model, 31, 28, 22, nt=40, seed=9, damping=F.DAMP_W3D)
     m.vdamp = F.VDAMP_16KM
     ref = O.run(m, 40, prec)
-    assert_bitwise(product(m, 40, prec), ref, "vdamp")
+    assert_bitwise(product(m, 40, prec, fused=form), ref, "vdamp")
     m.vdamp = 0.0
     undamped = O.run(m, 40, prec)
     assert not np.array_equal(undamped.traces, ref.traces)
@@ -151,6 +156,37 @@ def test_tiling_and_graph_do_not_change_results(cuda_device, kchunk, graph_steps
     m = I.random_small(F.MODEL_ORTHO, 40, 33, 29, nt=40, seed=11, damping=F.DAMP_SEPARABLE)
     ref = O.run(m, 40)
     assert_bitwise(product(m, 40, kchunk=kchunk, graph_steps=graph_steps, chunks=[13, 20, 7], fused=fused), ref)
+
+
+def test_wave_scheduler_settings(cuda_device):
+    """The wavefront step on a grid with hundreds of items per step (many CTAs in flight, velocity
+    items waiting on stress items): every lag and slab depth gives the oracle's bits, with
+    sources on tile and slab borders, and the autotuner's pick as well."""
+    m = I.random_small(F.MODEL_ORTHO, 100, 72, 48, nt=30, seed=23, damping=F.DAMP_W3D)
+    ent, coef = [], []
+    for comp in range(3, 9):
+        for (i, j, k) in ((31, 7, 3), (32, 8, 4), (64, 16, 7), (63, 15, 8), (99, 71, 2), (10, 40, 47)):
+            ent.append((comp, i, j, k))
+            coef.append(0.1 * (comp - 5) + 0.01 * i)
+    m.sources = np.array(ent, np.int32)
+    m.source_coef = np.array(coef)
+    ref = O.run(m, 30)
+    for lag in (1, 100, 100000):
+        for kchunk in (4, 7):
+            with Solver.from_model(m, fused=F.STEP_WAVE, kchunk=kchunk, graph_steps=8) as s:
+                s.set_wave(lag)
+                assert s.wave_lag() == lag
+                s.run(30)
+                got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+            assert_bitwise(got, ref, f"lag {lag} kchunk {kchunk}")
+    with Solver.from_model(m, fused=F.STEP_WAVE) as s:
+        s.autotune(4)
+        s.run(30)
+        got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+    assert_bitwise(got, ref, "autotuned")
+    with Solver.from_model(m) as s, pytest.raises(EwfError) as e:
+        s.set_wave(100)
+    assert e.value.status == -5
 
 
 def test_workload_shapes_small(cuda_device):
