@@ -191,6 +191,7 @@ struct ewf_handle {
     int wave_key[3] = {-1, -1, -1};  // (kslab, src_version, n) the grouping was built for
     int src_version = 0;
     int wave_lag_pct = 100;     // lag = ntx + 1 + CTAs * pct / 100 (autotuned)
+    int wave_hold = -1;         // diagnostic: stress item whose done flag is withheld
     void *comp_alloc[3] = {};
     void *m_alloc[12] = {};
     bool m_set[12] = {};
@@ -1059,6 +1060,7 @@ static void wave_entry(const ewf_handle *h, cudaEvent_t *ev, int)
     wa.nstf = (int)h->nstf;
     wa.it_ptr = h->d_it;
     wa.order = h->p.src_order;
+    wa.hold = h->wave_hold;
     if (ev) cudaEventRecord(ev[0], h->stream);
     kern<<<ctas, WAVE_THREADS, 0, h->stream>>>(a, wa);
     if (ev) {
@@ -1314,6 +1316,16 @@ extern "C" int ewf_set_wave(ewf_handle *h, int32_t lag_pct)
     if (!h->wave) return ewf_fail(EWF_ERR_STATE, "not a wavefront-step handle");
     if (lag_pct < 1 || lag_pct > 100000) return ewf_fail(EWF_ERR_ARG, "lag_pct must be in [1, 100000] (got %d)", lag_pct);
     h->wave_lag_pct = lag_pct;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_wave_hold(ewf_handle *h, int32_t item)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (!h->wave) return ewf_fail(EWF_ERR_STATE, "not a wavefront-step handle");
+    if (item < -1) return ewf_fail(EWF_ERR_ARG, "item must be >= -1");
+    h->wave_hold = item;
     h->graph_dirty = true;
     return EWF_OK;
 }

@@ -42,6 +42,7 @@ struct WaveArgs {
     int nstf;
     const int *it_ptr;
     int order;                 // injection semantics (k_inject)
+    int hold;                  // diagnostic: this stress item never publishes its flag (-1: none)
     WaveShape w;
 };
 
@@ -121,7 +122,7 @@ __device__ __forceinline__ void wave_publish(const StepArgs<T> &a, const WaveArg
         }
     }
     __threadfence();
-    st_release_gpu(&wa.done[idx], gen + 1);
+    if (idx != wa.hold) st_release_gpu(&wa.done[idx], gen + 1);
 }
 
 // MINB: CTAs per SM the register budget is sized for

@@ -75,6 +75,7 @@ SIGNATURES = {
     "ewf_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ewf_wave_hold": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_batch_create": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ewf_batch_destroy": (None, [C.c_void_p]),
     "ewf_batch_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t, C.c_int32]),
@@ -277,6 +278,10 @@ class Solver:
         """Wavefront step: lag of the velocity items behind the stress items, percent of the resident
         CTAs (the autotuner sets it; results do not depend on it)."""
         _check(self._lib.ewf_set_wave(self._h, int(lag_pct)), "ewf_set_wave")
+
+    def wave_hold(self, item: int) -> None:
+        """Diagnostic: stress item `item` never publishes its done flag (-1: normal operation)."""
+        _check(self._lib.ewf_wave_hold(self._h, int(item)), "ewf_wave_hold")
 
     def wave_lag(self) -> int:
         lag = C.c_int32()

@@ -202,6 +202,11 @@ int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
  * EWF_ERR_STATE for the other step forms. */
 int ewf_set_wave(ewf_handle *h, int32_t lag_pct);
 int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct);
+/* Diagnostic for tests of the failure path: stress item `item` of the wavefront step never
+ * publishes its done flag, so the velocity items that depend on it give up after their bounded
+ * wait and ewf_run returns EWF_ERR_CUDA (the state of that run is invalid; the handle stays
+ * usable after ewf_reset).  -1 restores normal operation. */
+int ewf_wave_hold(ewf_handle *h, int32_t item);
 
 /* Writes 0_infos.inf and 0_0_{Src,Rec,Rec_x,Rec_y,Rec_y2,Vx,Vy,Vz}.res into workdir
  * (OK4:521-532).  Rec* are the first four receivers. */

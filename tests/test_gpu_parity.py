@@ -189,6 +189,24 @@ def test_wave_scheduler_settings(cuda_device):
     assert e.value.status == -5
 
 
+def test_wave_wait_gives_up_and_handle_recovers(cuda_device):
+    """A done flag that nothing sets (withheld by the diagnostic hook): the velocity items waiting
+    for it give up after their bounded wait, ewf_run reports the failure instead of hanging, and
+    after a reset the same handle runs bit-exact again."""
+    m = I.random_small(F.MODEL_ORTHO, 64, 48, 24, nt=12, seed=31, damping=F.DAMP_W3D)
+    ref = O.run(m, 12)
+    with Solver.from_model(m, fused=F.STEP_WAVE, kchunk=4, graph_steps=-1) as s:
+        s.wave_hold(7)
+        with pytest.raises(EwfError) as e:
+            s.run(2)
+        assert e.value.status == -2 and "gave up" in str(e.value)
+        s.wave_hold(-1)
+        s.reset()
+        s.run(12)
+        got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+    assert_bitwise(got, ref, "after recovery")
+
+
 def test_workload_shapes_small(cuda_device):
     """The two benchmark workloads at reduced size, FP32, bit-exact."""
     m = I.iso_homogeneous(n=48, nt=120)
