@@ -1,8 +1,9 @@
 """Cache of the z-chunk autotuner's choices (JSON), so a workload is timed once per GPU model.
 
 The library's autotuner (`ewf_autotune`, `ewf_batch_autotune`) times the step for z-chunks of
-4..64 planes.  The best chunk depends on the GPU, the scheme (model, damping, precision, one-pass
-or two-kernel step) and the grid, not on the inputs' values, so it is stored under that key:
+4..64 planes.  The best chunk depends on the GPU, the scheme (model, damping, precision, step
+form) and the grid, not on the inputs' values, so it is stored under that key (the wavefront
+form's lag is re-tuned by `ewf_autotune` when a handle needs it):
 
     from elanfmt_gb300 import tuning
     k = tuning.kchunk_for(model, precision=F.PREC_F32)      # cached, or tuned once and stored
@@ -24,8 +25,11 @@ def cache_path() -> str:
                                                               "kchunk.json")
 
 
-def key(device_name: str, m, precision: int, fused: bool) -> str:
-    return (f"{device_name}|model{m.model}|damp{m.damping}|prec{precision}|{'fused' if fused else 'split'}|"
+FORM_NAMES = {F.STEP_SPLIT: "split", F.STEP_FUSED: "fused", F.STEP_WAVE: "wave"}
+
+
+def key(device_name: str, m, precision: int, form: int) -> str:
+    return (f"{device_name}|model{m.model}|damp{m.damping}|prec{precision}|{FORM_NAMES[int(form)]}|"
             f"{m.nx}x{m.ny}x{m.nz}")
 
 
@@ -51,10 +55,11 @@ def store(k: str, kchunk: int, path: str | None = None) -> None:
     os.replace(tmp, p)
 
 
-def kchunk_for(m, precision: int = F.PREC_F32, fused: bool = False, nsteps: int = 30, path: str | None = None,
+def kchunk_for(m, precision: int = F.PREC_F32, fused: int = F.STEP_SPLIT, nsteps: int = 30, path: str | None = None,
                device_name: str | None = None, tune=None) -> int:
-    """The cached z-chunk for this workload shape, or the autotuner's choice (then cached).
-    `tune(m, precision, fused, nsteps) -> int` replaces the GPU autotuner (tests)."""
+    """The cached z-chunk for this workload shape and step form (F.STEP_*), or the autotuner's
+    choice (then cached).  `tune(m, precision, form, nsteps) -> int` replaces the GPU autotuner
+    (tests)."""
     if device_name is None:
         import torch
 

@@ -20,8 +20,11 @@ def test_kchunk_cached_per_shape(tmp_path):
     assert tuning.kchunk_for(a, precision=F.PREC_F64, path=path, device_name="gpuX", tune=fake) == 12
     assert tuning.kchunk_for(a, path=path, device_name="gpuY", tune=fake) == 12
     assert len(calls) == 4                       # the repeated query was served from the file
+    for form in (F.STEP_FUSED, F.STEP_WAVE):     # every step form has its own entry
+        assert tuning.kchunk_for(a, fused=form, path=path, device_name="gpuX", tune=fake) == 12
+    assert len(calls) == 6
     data = tuning.load(path)
-    assert len(data) == 4 and all(isinstance(v, int) for v in data.values())
+    assert len(data) == 6 and all(isinstance(v, int) for v in data.values())
 
 
 def test_unreadable_cache_is_empty(tmp_path):
