@@ -116,10 +116,9 @@ struct StressIn {
     T pw[DAMP == DAMP_PERCOMP ? 6 : 1];  // per-component weights at the cell
 };
 
-// c: state index (x stride R), cm: material index of the same cell
+// State part of a cell's stress inputs (c: state index, x stride R).
 template <typename T, int MODEL, int DAMP, int RC, bool COH = false>
-__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k,
-                                            StressIn<T, MODEL, DAMP> &q)
+__device__ __forceinline__ void stress_load_state(const StepArgs<T> &a, long long c, StressIn<T, MODEL, DAMP> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
@@ -135,6 +134,12 @@ __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, l
     q.vz_jm = lds<COH>(a.f[2] + c - sx);
 #pragma unroll
     for (int f = 0; f < 6; ++f) q.s[f] = a.f[3 + f][c];
+}
+
+// Material part (moduli, damping) of a cell's stress inputs (cm: material index, plane k).
+template <typename T, int MODEL, int DAMP>
+__device__ __forceinline__ void stress_load_mat(const StepArgs<T> &a, long long cm, int k, StressIn<T, MODEL, DAMP> &q)
+{
     if (MODEL == MODEL_ISO) {
         q.c[0] = ld(a.m[0] + cm);
         q.c[1] = ld(a.m[1] + cm);
@@ -156,6 +161,127 @@ __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, l
         q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + cm) : ld(a.w1[2] + k);
     }
 }
+// c: state index (x stride R), cm: material index of the same cell
+template <typename T, int MODEL, int DAMP, int RC, bool COH = false>
+__device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k,
+                                            StressIn<T, MODEL, DAMP> &q)
+{
+    stress_load_state<T, MODEL, DAMP, RC, COH>(a, c, q);
+    stress_load_mat<T, MODEL, DAMP>(a, cm, k, q);
+}
+
+// damping factors constant along a column
+template <typename T>
+struct ColDamp {
+    T wavx, wavy, wxi, wyj, pxy;
+};
+template <typename T, int DAMP>
+__device__ __forceinline__ ColDamp<T> col_damp(const StepArgs<T> &a, int i, int j)
+{
+    ColDamp<T> d{T(0), T(0), T(0), T(0), T(0)};
+    if (DAMP == DAMP_PML1D) {
+        d.wxi = ld(a.w1[0] + i);
+        d.wyj = ld(a.w1[1] + j);
+        d.wavx = T(0.5) * (ld(a.w1[0] + i + 1) + d.wxi);
+        d.wavy = T(0.5) * (ld(a.w1[1] + j + 1) + d.wyj);
+    } else if (DAMP == DAMP_SEP) {
+        d.pxy = ld(a.w1[0] + i) * ld(a.w1[1] + j);
+    }
+    return d;
+}
+
+// The new stresses of cell (i, j, k): o = sxx syy szz sxy sxz syz; w_* = whether the shear
+// component is written there.  vx_m, vy_m: Vx, Vy at k-1; vz_k: Vz at k; wz_k: wz[k] (iso).
+template <typename T, int MODEL, int DAMP>
+__device__ __forceinline__ void stress_math(const StepArgs<T> &a, const StressIn<T, MODEL, DAMP> &q,
+                                            const ColDamp<T> &cd, int i, int j, int k, T vx_m, T vy_m, T vz_k,
+                                            T wz_k, T (&o)[6], bool &w_xy, bool &w_xz, bool &w_yz)
+{
+    const T dt = a.dt, rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
+    const T Vxx = (q.vx_ip - q.vx) * rdx;
+    const T Vyy = (q.vy_jp - q.vy) * rdy;
+    const T Vzz = (q.vz_p - vz_k) * rdz;
+    w_xy = true;
+    w_xz = true;
+    w_yz = true;
+    if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
+        const T c11 = q.c[0], c12 = q.c[1];
+        // DC_Earthquake FastWaveED_GPU3D_v1.cu:313-315: each component's own 3-D weight
+        o[0] = q.pw[0] * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
+        o[1] = q.pw[1] * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
+        o[2] = q.pw[2] * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
+        // :318-320, the shear moduli c66 (xy), c55 (xz), c44 (yz); guarded like ANISO
+        o[3] = q.pw[3] * (q.s[3] + a.c66 * dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
+        o[4] = q.pw[4] * (q.s[4] + a.c55 * dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
+        o[5] = q.pw[5] * (q.s[5] + a.c44 * dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
+        w_xy = (i > 0 && j > 0);
+        w_xz = (i > 0 && k > 0);
+        w_yz = (j > 0 && k > 0);
+    } else if (MODEL == MODEL_ISO) {
+        const T c11 = q.c[0], c12 = q.c[1];
+        // OK4:307-309
+        o[0] = cd.wavx * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
+        o[1] = cd.wavy * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
+        o[2] = T(0.5) * (q.w + wz_k) * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
+        const T c66dt = a.c66 * dt;
+        // OK4:323, 326, 329 (no guards: zero-padded neighbours at the low edges)
+        o[3] = wz_k * cd.wyj * cd.wxi * (q.s[3] + c66dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
+        o[4] = cd.wyj * wz_k * cd.wxi * (q.s[4] + c66dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
+        o[5] = cd.wxi * cd.wyj * wz_k * (q.s[5] + c66dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
+    } else if (MODEL == MODEL_ISOHET) {
+        const T W = (DAMP == DAMP_W3D) ? q.w : cd.pxy * q.w;
+        const T c11 = q.c[0], c12 = q.c[1];
+        // 9kmst.cu:316-318
+        o[0] = q.s[0] * W + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz);
+        o[1] = q.s[1] * W + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz);
+        o[2] = q.s[2] * W + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz);
+        // 9kmst.cu:321-325: edge shear moduli, derivatives times the reciprocal spacing
+        o[3] = q.s[3] * W + q.c[2] * dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy);
+        o[4] = q.s[4] * W + q.c[3] * dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz);
+        o[5] = q.s[5] * W + q.c[4] * dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy);
+        w_xy = (i > 0 && j > 0);
+        w_xz = (i > 0 && k > 0);
+        w_yz = (j > 0 && k > 0);
+    } else {
+        const T W = (DAMP == DAMP_W3D) ? q.w : cd.pxy * q.w;
+        // ANISO:312-325 (c[]: C11 C22 C33 C12 C13 C23 C66 C55 C44)
+        o[0] = q.s[0] * W + dt * (q.c[0] * Vxx + q.c[3] * Vyy + q.c[4] * Vzz);
+        o[1] = q.s[1] * W + dt * (q.c[3] * Vxx + q.c[1] * Vyy + q.c[5] * Vzz);
+        o[2] = q.s[2] * W + dt * (q.c[4] * Vxx + q.c[5] * Vyy + q.c[2] * Vzz);
+        // ANISO:327-352 (shear derivatives divide by the spacing)
+        const bool fd = a.fdiv != 0;
+        const T dVx_dy = div_spacing(q.vx - q.vx_jm, a.dy, a.rdy, fd);
+        const T dVy_dx = div_spacing(q.vy - q.vy_im, a.dx, a.rdx, fd);
+        o[3] = q.s[3] * W + dt * q.c[6] * (dVy_dx + dVx_dy);
+        const T dVx_dz = div_spacing(q.vx - vx_m, a.dz, a.rdz, fd);
+        const T dVz_dx = div_spacing(vz_k - q.vz_im, a.dx, a.rdx, fd);
+        o[4] = q.s[4] * W + dt * q.c[7] * (dVz_dx + dVx_dz);
+        const T dVy_dz = div_spacing(q.vy - vy_m, a.dz, a.rdz, fd);
+        const T dVz_dy = div_spacing(vz_k - q.vz_jm, a.dy, a.rdy, fd);
+        o[5] = q.s[5] * W + dt * q.c[8] * (dVy_dz + dVz_dy);
+        w_xy = (i > 0 && j > 0);
+        w_xz = (i > 0 && k > 0);
+        w_yz = (j > 0 && k > 0);
+    }
+}
+
+// Stores the new stresses of cell c (plane k; sys: state plane pitch), with BC1: szz = 0 on plane
+// 0 and, from the freshly updated plane 2, sxz / syz on plane 1 (OK4:279-282).
+template <typename T>
+__device__ __forceinline__ void stress_store(const StepArgs<T> &a, long long c, long long sys, int k, int i, int j,
+                                             bool row_bc, const T (&o)[6], bool w_xy, bool w_xz, bool w_yz)
+{
+    a.f[3][c] = o[0];
+    a.f[4][c] = o[1];
+    a.f[5][c] = (k == 0 && row_bc) ? T(0) : o[2];
+    if (w_xy) a.f[6][c] = o[3];
+    if (w_xz) a.f[7][c] = o[4];
+    if (w_yz) a.f[8][c] = o[5];
+    if (k == 2) {
+        if (i > 0 && row_bc) a.f[7][c - sys] = a.third * o[4];
+        if (j > 0) a.f[8][c - sys] = a.third * o[5];
+    }
+}
 
 // The column (X = i*R + r, j) over planes [k0, k1): X runs over the cells of every RHS.
 // RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
@@ -170,18 +296,7 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
     if (i >= a.nx || j >= a.ny) return;
     const int sxs = (RC == 1) ? a.sx : a.sxs;
     const long long sys = (RC == 1) ? a.sy : a.sys, sy = a.sy;
-    const T dt = a.dt, rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
-
-    // damping factors constant along the column
-    T wavx = T(0), wavy = T(0), wxi = T(0), wyj = T(0), pxy = T(0);
-    if (DAMP == DAMP_PML1D) {
-        wxi = ld(a.w1[0] + i);
-        wyj = ld(a.w1[1] + j);
-        wavx = T(0.5) * (ld(a.w1[0] + i + 1) + wxi);
-        wavy = T(0.5) * (ld(a.w1[1] + j + 1) + wyj);
-    } else if (DAMP == DAMP_SEP) {
-        pxy = ld(a.w1[0] + i) * ld(a.w1[1] + j);
-    }
+    const ColDamp<T> cd = col_damp<T, DAMP>(a, i, j);
     const bool row_bc = (j < a.bc1_rows);
 
     long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys + (SOFF ? soff : 0);
@@ -198,82 +313,11 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
         if (SEP && k > k0) cm += sy;
         const StressIn<T, MODEL, DAMP> q = nxt;
         if (k + 1 < k1) stress_load<T, MODEL, DAMP, RC, COH>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
-        const T Vxx = (q.vx_ip - q.vx) * rdx;
-        const T Vyy = (q.vy_jp - q.vy) * rdy;
-        const T Vzz = (q.vz_p - vz_k) * rdz;
-        T sxx, syy, szz, sxy, sxz, syz;
-        bool w_xy = true, w_xz = true, w_yz = true;
-        if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
-            const T c11 = q.c[0], c12 = q.c[1];
-            // DC_Earthquake FastWaveED_GPU3D_v1.cu:313-315: each component's own 3-D weight
-            sxx = q.pw[0] * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
-            syy = q.pw[1] * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
-            szz = q.pw[2] * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
-            // :318-320, the shear moduli c66 (xy), c55 (xz), c44 (yz); guarded like ANISO
-            sxy = q.pw[3] * (q.s[3] + a.c66 * dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
-            sxz = q.pw[4] * (q.s[4] + a.c55 * dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
-            syz = q.pw[5] * (q.s[5] + a.c44 * dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
-            w_xy = (i > 0 && j > 0);
-            w_xz = (i > 0 && k > 0);
-            w_yz = (j > 0 && k > 0);
-        } else if (MODEL == MODEL_ISO) {
-            const T c11 = q.c[0], c12 = q.c[1];
-            // OK4:307-309
-            sxx = wavx * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
-            syy = wavy * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
-            szz = T(0.5) * (q.w + wz_k) * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
-            const T c66dt = a.c66 * dt;
-            // OK4:323, 326, 329 (no guards: zero-padded neighbours at the low edges)
-            sxy = wz_k * wyj * wxi * (q.s[3] + c66dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
-            sxz = wyj * wz_k * wxi * (q.s[4] + c66dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
-            syz = wxi * wyj * wz_k * (q.s[5] + c66dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy));
-            wz_k = q.w;
-        } else if (MODEL == MODEL_ISOHET) {
-            const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
-            const T c11 = q.c[0], c12 = q.c[1];
-            // 9kmst.cu:316-318
-            sxx = q.s[0] * W + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz);
-            syy = q.s[1] * W + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz);
-            szz = q.s[2] * W + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz);
-            // 9kmst.cu:321-325: edge shear moduli, derivatives times the reciprocal spacing
-            sxy = q.s[3] * W + q.c[2] * dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy);
-            sxz = q.s[4] * W + q.c[3] * dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz);
-            syz = q.s[5] * W + q.c[4] * dt * ((q.vy - vy_m) * rdz + (vz_k - q.vz_jm) * rdy);
-            w_xy = (i > 0 && j > 0);
-            w_xz = (i > 0 && k > 0);
-            w_yz = (j > 0 && k > 0);
-        } else {
-            const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
-            // ANISO:312-325 (c[]: C11 C22 C33 C12 C13 C23 C66 C55 C44)
-            sxx = q.s[0] * W + dt * (q.c[0] * Vxx + q.c[3] * Vyy + q.c[4] * Vzz);
-            syy = q.s[1] * W + dt * (q.c[3] * Vxx + q.c[1] * Vyy + q.c[5] * Vzz);
-            szz = q.s[2] * W + dt * (q.c[4] * Vxx + q.c[5] * Vyy + q.c[2] * Vzz);
-            // ANISO:327-352 (shear derivatives divide by the spacing)
-            const bool fd = a.fdiv != 0;
-            const T dVx_dy = div_spacing(q.vx - q.vx_jm, a.dy, a.rdy, fd);
-            const T dVy_dx = div_spacing(q.vy - q.vy_im, a.dx, a.rdx, fd);
-            sxy = q.s[3] * W + dt * q.c[6] * (dVy_dx + dVx_dy);
-            const T dVx_dz = div_spacing(q.vx - vx_m, a.dz, a.rdz, fd);
-            const T dVz_dx = div_spacing(vz_k - q.vz_im, a.dx, a.rdx, fd);
-            sxz = q.s[4] * W + dt * q.c[7] * (dVz_dx + dVx_dz);
-            const T dVy_dz = div_spacing(q.vy - vy_m, a.dz, a.rdz, fd);
-            const T dVz_dy = div_spacing(vz_k - q.vz_jm, a.dy, a.rdy, fd);
-            syz = q.s[5] * W + dt * q.c[8] * (dVy_dz + dVz_dy);
-            w_xy = (i > 0 && j > 0);
-            w_xz = (i > 0 && k > 0);
-            w_yz = (j > 0 && k > 0);
-        }
-        a.f[3][c] = sxx;
-        a.f[4][c] = syy;
-        a.f[5][c] = (k == 0 && row_bc) ? T(0) : szz;
-        if (w_xy) a.f[6][c] = sxy;
-        if (w_xz) a.f[7][c] = sxz;
-        if (w_yz) a.f[8][c] = syz;
-        // BC1 plane 1 from the freshly updated plane 2 (OK4:281-282)
-        if (k == 2) {
-            if (i > 0 && row_bc) a.f[7][c - sys] = a.third * sxz;
-            if (j > 0) a.f[8][c - sys] = a.third * syz;
-        }
+        T o[6];
+        bool w_xy, w_xz, w_yz;
+        stress_math<T, MODEL, DAMP>(a, q, cd, i, j, k, vx_m, vy_m, vz_k, wz_k, o, w_xy, w_xz, w_yz);
+        stress_store<T>(a, c, sys, k, i, j, row_bc, o, w_xy, w_xz, w_yz);
+        if (MODEL == MODEL_ISO && DAMP == DAMP_PML1D) wz_k = q.w;
         vx_m = q.vx;
         vy_m = q.vy;
         vz_k = q.vz_p;
@@ -339,9 +383,10 @@ struct VelIn {
     T cp[KAHAN ? 3 : 1];
 };
 
+// State part of a cell's velocity inputs (c: state index, x stride R): the stresses around the
+// cell and the old velocities.
 template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool COH = false>
-__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k,
-                                         VelIn<T, MODEL, DAMP, KAHAN> &q)
+__device__ __forceinline__ void vel_load_state(const StepArgs<T> &a, long long c, VelIn<T, MODEL, DAMP, KAHAN> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
@@ -360,6 +405,12 @@ __device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long
     q.syz_jp = lds<COH>(a.f[8] + c + sx);
 #pragma unroll
     for (int f = 0; f < 3; ++f) q.v[f] = a.f[f][c];
+}
+
+// Material part (buoyancy, damping) of a cell's velocity inputs (cm: material index, plane k).
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+__device__ __forceinline__ void vel_load_mat(const StepArgs<T> &a, long long cm, int k, VelIn<T, MODEL, DAMP, KAHAN> &q)
+{
     if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
 #pragma unroll
         for (int f = 0; f < 3; ++f) q.pw[f] = ld(a.w6[f] + cm);
@@ -370,6 +421,13 @@ __device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long
         for (int f = 0; f < 3; ++f) q.b[f] = ld(a.m[9 + f] + cm);
         q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + cm) : ld(a.w1[2] + k);
     }
+}
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool COH = false>
+__device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k,
+                                         VelIn<T, MODEL, DAMP, KAHAN> &q)
+{
+    vel_load_state<T, MODEL, DAMP, KAHAN, RC, COH>(a, c, q);
+    vel_load_mat<T, MODEL, DAMP, KAHAN>(a, cm, k, q);
     if (KAHAN) {
 #pragma unroll
         for (int f = 0; f < 3; ++f) q.cp[f] = a.comp[f][c];
@@ -393,6 +451,71 @@ __device__ __forceinline__ T vel_update(const StepArgs<T> &a, T V, T dS, T w_or_
     return t;
 }
 
+// damping factors constant along a velocity column
+template <typename T>
+struct VelDamp {
+    T wxm, wym, pxy;
+};
+template <typename T, int DAMP>
+__device__ __forceinline__ VelDamp<T> vel_damp(const StepArgs<T> &a, int i, int j)
+{
+    VelDamp<T> d{T(0), T(0), T(0)};
+    if (DAMP == DAMP_PML1D) {
+        d.wxm = ld(a.w1[0] + i - 1);
+        d.wym = ld(a.w1[1] + j - 1);
+    } else if (DAMP == DAMP_SEP) {
+        d.pxy = ld(a.w1[0] + i) * ld(a.w1[1] + j);
+    }
+    return d;
+}
+
+// The new velocities of one cell: v = Vx Vy Vz (cp: Kahan compensations, updated in place).
+// szz_m: szz at k-1; sxz_k, syz_k: sxz, syz at k.
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+__device__ __forceinline__ void vel_math(const StepArgs<T> &a, const VelIn<T, MODEL, DAMP, KAHAN> &q,
+                                         const VelDamp<T> &vd, T szz_m, T sxz_k, T syz_k, T (&v)[3], T (&cp)[3])
+{
+    const T rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
+    const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
+    const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
+    const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;
+    T ax, ay, az, bx, by, bz;
+    if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
+        // DC_Earthquake FastWaveED_GPU3D_v1.cu:344-360: each component's own 3-D weight
+        ax = q.pw[0]; ay = q.pw[1]; az = q.pw[2];
+        bx = a.bx; by = a.by; bz = a.bz;
+    } else if (MODEL == MODEL_ISO) {
+        ax = vd.wxm; ay = vd.wym; az = q.w;
+        bx = a.bx; by = a.by; bz = a.bz;
+    } else {
+        const T W = (DAMP == DAMP_W3D) ? q.w : vd.pxy * q.w;
+        ax = ay = az = W;
+        bx = q.b[0]; by = q.b[1]; bz = q.b[2];
+    }
+    v[0] = vel_update<T, MODEL, KAHAN>(a, q.v[0], dSx, ax, bx, cp[0]);
+    v[1] = vel_update<T, MODEL, KAHAN>(a, q.v[1], dSy, ay, by, cp[1]);
+    v[2] = vel_update<T, MODEL, KAHAN>(a, q.v[2], dSz, az, bz, cp[2]);
+}
+
+// Stores the new velocities of cell c on plane k, within the ranges OK4:358, 365, 372.
+template <typename T, bool KAHAN>
+__device__ __forceinline__ void vel_store(const StepArgs<T> &a, long long c, int k, int i, int j, const T (&v)[3],
+                                          const T (&cp)[3])
+{
+    if (j < a.ny - 1 && k < a.nz - 1) {
+        a.f[0][c] = v[0];
+        if (KAHAN) a.comp[0][c] = cp[0];
+    }
+    if (i < a.nx - 1 && k < a.nz - 1) {
+        a.f[1][c] = v[1];
+        if (KAHAN) a.comp[1][c] = cp[1];
+    }
+    if (i < a.nx - 1 && j < a.ny - 1) {
+        a.f[2][c] = v[2];
+        if (KAHAN) a.comp[2][c] = cp[2];
+    }
+}
+
 template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, bool COH = false>
 __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0)
 {
@@ -405,20 +528,7 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
     if (k0 >= k1) return;
     const int sxs = (RC == 1) ? a.sx : a.sxs;
     const long long sys = (RC == 1) ? a.sy : a.sys, sy = a.sy;
-    const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const T rdx = a.rdx, rdy = a.rdy, rdz = a.rdz;
-
-    const bool do_x = (j < ny - 1);
-    const bool do_y = (i < nx - 1);
-    const bool do_z = (i < nx - 1) && (j < ny - 1);
-
-    T wxm = T(0), wym = T(0), pxy = T(0);
-    if (DAMP == DAMP_PML1D) {
-        wxm = ld(a.w1[0] + i - 1);
-        wym = ld(a.w1[1] + j - 1);
-    } else if (DAMP == DAMP_SEP) {
-        pxy = ld(a.w1[0] + i) * ld(a.w1[1] + j);
-    }
+    const VelDamp<T> vd = vel_damp<T, DAMP>(a, i, j);
 
     long long c = (long long)X + (long long)j * sxs + (long long)k0 * sys + (SOFF ? soff : 0);
     long long cm = !SEP ? c : (RC == 1) ? c - soff : (long long)i + (long long)j * a.sx + (long long)k0 * sy;
@@ -432,39 +542,9 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
         if (SEP && k > k0) cm += sy;
         VelIn<T, MODEL, DAMP, KAHAN> q = nxt;
         if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
-        const T dSx = (q.sxx - q.sxx_im) * rdx + (q.sxy_jp - q.sxy) * rdy + (q.sxz_p - sxz_k) * rdz;
-        const T dSy = (q.syy - q.syy_jm) * rdy + (q.sxy_ip - q.sxy) * rdx + (q.syz_p - syz_k) * rdz;
-        const T dSz = (q.szz - szz_m) * rdz + (q.sxz_ip - sxz_k) * rdx + (q.syz_jp - syz_k) * rdy;
-        T ax, ay, az, bx, by, bz;
-        if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP) {
-            // DC_Earthquake FastWaveED_GPU3D_v1.cu:344-360: each component's own 3-D weight
-            ax = q.pw[0]; ay = q.pw[1]; az = q.pw[2];
-            bx = a.bx; by = a.by; bz = a.bz;
-        } else if (MODEL == MODEL_ISO) {
-            ax = wxm; ay = wym; az = q.w;
-            bx = a.bx; by = a.by; bz = a.bz;
-        } else {
-            const T W = (DAMP == DAMP_W3D) ? q.w : pxy * q.w;
-            ax = ay = az = W;
-            bx = q.b[0]; by = q.b[1]; bz = q.b[2];
-        }
-        T cpx = KAHAN ? q.cp[0] : T(0), cpy = KAHAN ? q.cp[1] : T(0), cpz = KAHAN ? q.cp[2] : T(0);
-        const T vx = vel_update<T, MODEL, KAHAN>(a, q.v[0], dSx, ax, bx, cpx);
-        const T vy = vel_update<T, MODEL, KAHAN>(a, q.v[1], dSy, ay, by, cpy);
-        const T vz = vel_update<T, MODEL, KAHAN>(a, q.v[2], dSz, az, bz, cpz);
-        // ranges OK4:358, 365, 372
-        if (do_x && k < nz - 1) {
-            a.f[0][c] = vx;
-            if (KAHAN) a.comp[0][c] = cpx;
-        }
-        if (do_y && k < nz - 1) {
-            a.f[1][c] = vy;
-            if (KAHAN) a.comp[1][c] = cpy;
-        }
-        if (do_z) {
-            a.f[2][c] = vz;
-            if (KAHAN) a.comp[2][c] = cpz;
-        }
+        T v[3], cp[3] = {KAHAN ? q.cp[0] : T(0), KAHAN ? q.cp[1] : T(0), KAHAN ? q.cp[2] : T(0)};
+        vel_math<T, MODEL, DAMP, KAHAN>(a, q, vd, szz_m, sxz_k, syz_k, v, cp);
+        vel_store<T, KAHAN>(a, c, k, i, j, v, cp);
         szz_m = q.szz;
         sxz_k = q.sxz_p;
         syz_k = q.syz_p;
