@@ -467,7 +467,8 @@ def main_reference(args):
     total = sum(times)
     value = m.cells * per * args.steps / total / 1e9
     sample = f"{per} time steps of the full {m.nx}x{m.ny}x{m.nz} grid per bench step, FP64"
-    out = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": 0,
+    # n_gpus mirrors the launch (--gpus); the work itself runs on rank 0's host cores (cpu_baseline)
+    out = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded)", "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": m.nt},
