@@ -3,9 +3,9 @@
 // A small MLP maps (source x, y, depth, receiver offset, azimuth) to the 6 x 3 x nt elementary
 // Green's-function seismograms; the solver generates its training data and measures its error.
 // Everything here works on caller-owned device buffers (plain pointers):
-//   ewf_mlp_gemm        C[M,N] = A[M,K] . B[N,K]^T (+ bias), bf16 operands on the tensor cores
-//                       (mma.sync m16n8k16, fp32 accumulation), epilogue: fp32 out, bf16 out,
-//                       pre-activation out, GELU
+//   ewf_mlp_gemm        C[M,N] = A[M,K] . B[N,K]^T (+ bias), bf16 operands on the tcgen05 tensor
+//                       cores (TMA-fed, fp32 accumulator in tensor memory), epilogue: fp32 out,
+//                       bf16 out, pre-activation out, GELU
 //   ewf_mlp_transpose   bf16 [R,C] -> [C,R] (so every product is an A.B^T GEMM)
 //   ewf_mlp_gelu_grad   dX = dY * GELU'(pre)  (bf16 out)
 //   ewf_mlp_bias_grad   db[n] = sum_m dY[m,n]
@@ -13,43 +13,19 @@
 //   ewf_mlp_adam        Adam step on fp32 master weights, refreshing the bf16 copy
 //   ewf_mlp_combine     out[m,o,t] = sum_f R[m,o,f] G[m,f,t]: per-sample mixing of the predicted
 //                       fundamental traces into the 18 moment-tensor x component traces
-// Tile sizes require M, N multiples of 128 and K a multiple of 32 (checked).
+// The GEMM requires M, N multiples of 128 and K a multiple of 32 (checked).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ewf_umma.h"
 #include "ewfd.h"
 #include "ewfd_internal.h"
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 32, PAD = 8;
-constexpr int LDS = BK + PAD;  // bf16 elements per smem row
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
-
-__device__ __forceinline__ void ldmatrix_x4(uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3, const void *p)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(smem_u32(p)));
-}
-
-__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, const uint32_t *b)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 
@@ -60,102 +36,225 @@ __device__ __forceinline__ float gelu_grad(float x)
     return cdf + x * pdf;
 }
 
-// 256 threads = 8 warps as 2 (M) x 4 (N); warp tile 64 x 32 = 4 x 4 mma tiles of 16 x 8.
-__global__ void __launch_bounds__(256) k_gemm_nt(const __nv_bfloat16 *__restrict__ A, const __nv_bfloat16 *__restrict__ B,
-                                                  const float *__restrict__ bias, float *__restrict__ Cf,
-                                                  __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Pre, int M, int N,
-                                                  int K, int act)
+// ---------------------------------------------------------------------------------------------
+// tcgen05 GEMM: C[M,N] = A[M,K] . B[N,K]^T on the 5th-generation tensor cores.  One CTA per
+// 128 x BN tile of C (BN = 256, or 128 when N is not a multiple of 256); the fp32 accumulator
+// lives in tensor memory (128 lanes x BN columns).  Warp roles, 128 threads:
+//   warp 0, one lane: TMA producer -- per k-stage one 2-D bulk tensor copy per operand (128-byte
+//     swizzle, ewf_umma.h) into the free stage, completing on that stage's "full" mbarrier;
+//   warp 1, one lane: MMA issuer -- waits for "full", issues 4 tcgen05.mma (K = 16 each) and
+//     commits them to the stage's "empty" mbarrier (which frees it for the producer), and after
+//     the last stage to "done";
+//   all 4 warps: epilogue -- wait for "done", read the accumulator with tcgen05.ld (warp w: rows
+//     32w .. 32w+31), add the bias, GELU, write the requested outputs.
+// K beyond the last full stage is read as zeros (the tensor map's out-of-bounds fill), so any K
+// that is a multiple of 8 works.  Every mbarrier wait is bounded: on timeout the wait raises
+// g_umma_err and gives up (the outputs of that launch are then invalid, ewf_mlp_status reports
+// it); the CTA still frees its tensor memory and returns.
+// ---------------------------------------------------------------------------------------------
+__device__ int g_umma_err = 0;
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count)
 {
-    __shared__ __align__(16) __nv_bfloat16 As[2][BM][LDS];
-    __shared__ __align__(16) __nv_bfloat16 Bs[2][BN][LDS];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp >> 2, wn = warp & 3;  // warp position
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(b)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity)
+{
+    for (int i = 0; i < (1 << 22); ++i)
+        if (mbar_try_wait(b, parity)) return true;
+    atomicExch(&g_umma_err, 1);
+    return false;
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+                     smem_u32(dst)),
+                 "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-    float acc[4][4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t accum)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+                 "l"(da), "l"(db), "r"(idesc), "r"(accum)
+                 : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *b)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
+                 : "memory");
+}
+// 16 consecutive fp32 accumulator columns of this thread's lane (load and wait in one block so
+// no use of the values can be scheduled before the wait)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                   "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                 : "r"(taddr)
+                 : "memory");
+}
 
-    // each thread copies 2 x 16 B of A and of B per stage: row = chunk / 4, col = (chunk % 4) * 8
-    auto load_stage = [&](int st, int k0) {
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int ch = tid + q * 256;
-            const int r = ch >> 2, cc = (ch & 3) * 8;
-            cp_async16(&As[st][r][cc], A + (size_t)(m0 + r) * K + k0 + cc);
-            cp_async16(&Bs[st][r][cc], B + (size_t)(n0 + r) * K + k0 + cc);
+template <int BN>
+__global__ void __launch_bounds__(ewf_umma::THREADS, 1)
+    k_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+           const float *__restrict__ bias, float *__restrict__ Cf, __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Pre,
+           int M, int N, int K, int act)
+{
+    namespace U = ewf_umma;
+    constexpr int STAGE = U::a_bytes() + BN * U::ROW_BYTES;
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ uint64_t full[U::STAGES], empty[U::STAGES], done;
+    __shared__ uint32_t s_tmem;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.y * U::BM, n0 = blockIdx.x * BN;
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);  // stage tiles on 1024 B
+
+    if (tid == 0) {
+        for (int s = 0; s < U::STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
         }
-        cp_async_commit();
-    };
-
-    const int nk = K / BK;
-    load_stage(0, 0);
-    for (int kt = 0; kt < nk; ++kt) {
-        const int st = kt & 1;
-        cp_async_wait_all();
-        __syncthreads();
-        if (kt + 1 < nk) load_stage(st ^ 1, (kt + 1) * BK);
-#pragma unroll
-        for (int kk = 0; kk < BK; kk += 16) {
-            uint32_t af[4][4], bfr[4][2];
-#pragma unroll
-            for (int mi = 0; mi < 4; ++mi) {
-                const int row = wm * 64 + mi * 16 + (lane & 15);
-                const int col = kk + (lane >> 4) * 8;
-                ldmatrix_x4(af[mi][0], af[mi][1], af[mi][2], af[mi][3], &As[st][row][col]);
-            }
-#pragma unroll
-            for (int nj = 0; nj < 4; nj += 2) {
-                // two n8 tiles: matrices (n 0-7, k 0-7), (n 0-7, k 8-15), (n 8-15, k 0-7), (n 8-15, k 8-15)
-                const int row = wn * 32 + nj * 8 + (lane & 7) + ((lane >> 4) << 3);
-                const int col = kk + ((lane >> 3) & 1) * 8;
-                uint32_t r0, r1, r2, r3;
-                ldmatrix_x4(r0, r1, r2, r3, &Bs[st][row][col]);
-                bfr[nj][0] = r0;
-                bfr[nj][1] = r1;
-                bfr[nj + 1][0] = r2;
-                bfr[nj + 1][1] = r3;
-            }
-#pragma unroll
-            for (int mi = 0; mi < 4; ++mi)
-#pragma unroll
-                for (int nj = 0; nj < 4; ++nj) mma_bf16(acc[mi][nj], af[mi], bfr[nj]);
-        }
-        __syncthreads();
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // epilogue
+    if (warp == 0) {
+        __syncwarp();  // the alloc is warp-collective (.sync.aligned)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)), "r"(BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const int nk = (K + U::BK - 1) / U::BK;
+
+    if (warp == 0 && lane == 0) {  // TMA producer
+        for (int kt = 0; kt < nk; ++kt) {
+            const int s = kt % U::STAGES;
+            if (kt >= U::STAGES && !mbar_wait(&empty[s], ((kt / U::STAGES) - 1) & 1)) break;
+            uint8_t *As = smem + s * STAGE;
+            mbar_expect_tx(&full[s], STAGE);
+            tma_load_2d(As, &mapA, kt * U::BK, m0, &full[s]);
+            tma_load_2d(As + U::a_bytes(), &mapB, kt * U::BK, n0, &full[s]);
+        }
+    } else if (warp == 1 && lane == 0) {  // MMA issuer
+        const uint32_t idesc = U::instr_desc_bf16_f32(U::BM, BN);
+        int kt = 0;
+        for (; kt < nk; ++kt) {
+            const int s = kt % U::STAGES;
+            if (!mbar_wait(&full[s], (kt / U::STAGES) & 1)) break;
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(smem + s * STAGE), b0 = a0 + U::a_bytes();
+            for (int j = 0; j < U::BK / U::MMA_K; ++j)
+                umma_bf16(tmem, U::smem_desc_sw128(a0 + 32 * j), U::smem_desc_sw128(b0 + 32 * j), idesc,
+                          (kt > 0 || j > 0) ? 1u : 0u);
+            umma_commit(&empty[s]);
+        }
+        umma_commit(&done);  // tracks every MMA issued before it
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(&done, 0);
+    tc_fence_after();
+
+    // epilogue: warp w owns accumulator lanes (rows) 32w .. 32w + 31
+    const int row = m0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+        float x[16];
 #pragma unroll
-    for (int mi = 0; mi < 4; ++mi)
+        for (int q = 0; q < 16; ++q) {
+            x[q] = ok ? __uint_as_float(v[q]) : __int_as_float(0x7fc00000);
+            if (bias) x[q] += bias[n0 + c0 + q];
+        }
+        const size_t o = (size_t)row * N + n0 + c0;
+        if (Pre)
 #pragma unroll
-        for (int nj = 0; nj < 4; ++nj)
+            for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4 *>(Pre + o + q) = make_float4(x[q], x[q + 1], x[q + 2], x[q + 3]);
+        if (act == 1)
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int row = m0 + wm * 64 + mi * 16 + (lane >> 2) + h * 8;
-                const int col = n0 + wn * 32 + nj * 8 + (lane & 3) * 2;
-                float v0 = acc[mi][nj][2 * h], v1 = acc[mi][nj][2 * h + 1];
-                if (bias) {
-                    v0 += bias[col];
-                    v1 += bias[col + 1];
-                }
-                const size_t o = (size_t)row * N + col;
-                if (Pre) {
-                    Pre[o] = v0;
-                    Pre[o + 1] = v1;
-                }
-                if (act == 1) {
-                    v0 = gelu(v0);
-                    v1 = gelu(v1);
-                }
-                if (Cf) {
-                    Cf[o] = v0;
-                    Cf[o + 1] = v1;
-                }
-                if (Cb) *reinterpret_cast<__nv_bfloat162 *>(Cb + o) = __floats2bfloat162_rn(v0, v1);
-            }
+            for (int q = 0; q < 16; ++q) x[q] = gelu(x[q]);
+        if (Cf)
+#pragma unroll
+            for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4 *>(Cf + o + q) = make_float4(x[q], x[q + 1], x[q + 2], x[q + 3]);
+        if (Cb)
+#pragma unroll
+            for (int q = 0; q < 16; q += 2) *reinterpret_cast<__nv_bfloat162 *>(Cb + o + q) = __floats2bfloat162_rn(x[q], x[q + 1]);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+    }
+}
+
+int check(cudaError_t e, const char *what);
+
+// 2-D tensor map of a K-major bf16 operand [rows, K] with boxes of BK x box_rows and the 128-byte swizzle
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int operand_map(CUtensorMap *m, const void *ptr, int rows, int K, int box_rows)
+{
+    static EncodeTiledFn enc = nullptr;
+    if (!enc) {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            !fn || q != cudaDriverEntryPointSuccess)
+            return ewf_fail(EWF_ERR_CUDA, "gemm: cuTensorMapEncodeTiled unavailable");
+        enc = (EncodeTiledFn)fn;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)ewf_umma::BK, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? EWF_OK : ewf_fail(EWF_ERR_ARG, "gemm: tensor map rejected (CUresult %d)", (int)r);
+}
+
+template <int BN>
+int launch_gemm(const void *A, const void *B, const float *bias, float *Cf, void *Cb, float *pre, int M, int N, int K,
+                int act, cudaStream_t stream)
+{
+    static bool attr = false;
+    const int smem = ewf_umma::smem_bytes(BN);
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return check(e, "gemm smem attribute");
+        attr = true;
+    }
+    alignas(64) CUtensorMap ma, mb;
+    int st = operand_map(&ma, A, M, K, ewf_umma::BM);
+    if (st) return st;
+    if ((st = operand_map(&mb, B, N, K, BN))) return st;
+    k_gemm<BN><<<dim3(N / BN, M / ewf_umma::BM), ewf_umma::THREADS, smem, stream>>>(
+        ma, mb, bias, Cf, (__nv_bfloat16 *)Cb, pre, M, N, K, act);
+    return check(cudaGetLastError(), "gemm launch");
 }
 
 __global__ void k_transpose(const __nv_bfloat16 *__restrict__ in, __nv_bfloat16 *__restrict__ out, int R, int Cc)
@@ -260,12 +359,26 @@ extern "C" int ewf_mlp_gemm(const void *A, const void *B, const float *bias, flo
                             int32_t N, int32_t K, int32_t act, void *stream)
 {
     if (!A || !B || (!Cf && !Cb && !pre)) return ewf_fail(EWF_ERR_ARG, "gemm: NULL operand");
-    if (M <= 0 || N <= 0 || K <= 0 || M % BM || N % BN || K % BK)
-        return ewf_fail(EWF_ERR_ARG, "gemm: M, N must be multiples of %d and K of %d (got %d %d %d)", BM, BK, M, N, K);
+    if (M <= 0 || N <= 0 || K <= 0 || M % 128 || N % 128 || K % 32)
+        return ewf_fail(EWF_ERR_ARG, "gemm: M, N must be multiples of 128 and K of 32 (got %d %d %d)", M, N, K);
     if (act != 0 && act != 1) return ewf_fail(EWF_ERR_ARG, "gemm: act must be 0 or 1");
-    k_gemm_nt<<<dim3(N / BN, M / BM), 256, 0, (cudaStream_t)stream>>>(
-        (const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias, Cf, (__nv_bfloat16 *)Cb, pre, M, N, K, act);
-    return check(cudaGetLastError(), "gemm launch");
+    if (((uintptr_t)A | (uintptr_t)B) & 15) return ewf_fail(EWF_ERR_ARG, "gemm: A and B must be 16-byte aligned");
+    if (((uintptr_t)Cf | (uintptr_t)pre) & 15 || (uintptr_t)Cb & 3) return ewf_fail(EWF_ERR_ARG, "gemm: outputs misaligned");
+    if (N % 256 == 0) return launch_gemm<256>(A, B, bias, Cf, Cb, pre, M, N, K, act, (cudaStream_t)stream);
+    return launch_gemm<128>(A, B, bias, Cf, Cb, pre, M, N, K, act, (cudaStream_t)stream);
+}
+
+extern "C" int ewf_mlp_status(void)
+{
+    int e = 0;
+    cudaError_t ce = cudaMemcpyFromSymbol(&e, g_umma_err, sizeof(int));
+    if (ce != cudaSuccess) return check(ce, "gemm status");
+    if (e) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_umma_err, &zero, sizeof(int));
+        return ewf_fail(EWF_ERR_CUDA, "gemm: an mbarrier wait gave up (outputs of that launch are invalid)");
+    }
+    return EWF_OK;
 }
 
 extern "C" int ewf_mlp_transpose(const void *in, void *out, int32_t rows, int32_t cols, void *stream)

@@ -614,9 +614,45 @@ def gemm_benchmark(shapes=((4096, 12800, 512), (4096, 512, 512), (256, 12800, 51
     return out
 
 
+def infer_benchmark(nq: int = 4096, nt: int = 1280, hidden: int = 512, layers: int = 4, reps: int = 20) -> dict:
+    """GF sets/s of surrogate inference at the study's network size, with random weights and
+    inputs: the forward pass (ewf_mlp_gemm, batches of 1024 queries as in MLP.predict) and the
+    azimuthal mixing (ewf_mlp_combine) of nq queries, timed with CUDA events as in study()."""
+    import torch
+
+    lib = load_library()
+    net = MLP([IN_PAD] + [hidden] * layers + [NFUND * nt], seed=1, fan_in0=4)
+    g = torch.Generator(device="cpu").manual_seed(2)
+    X = torch.randn(nq, IN_PAD, generator=g).to(torch.bfloat16).cuda()
+    R = torch.randn(nq, NCOMP, NFUND, generator=g).cuda()
+    out = torch.empty(nq, NCOMP * nt, device="cuda")
+
+    def infer():
+        y = net.predict(X)
+        for a in range(0, nq, 32768):
+            b = min(a + 32768, nq)
+            _check(lib.ewf_mlp_combine(_p(R[a:b]), _p(y[a:b]), _p(out[a:b]), b - a, NCOMP, NFUND, nt, _stream()),
+                   "ewf_mlp_combine")
+
+    infer()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        infer()
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) * 1e-3 / reps
+    _check(lib.ewf_mlp_status(), "ewf_mlp_status")
+    return {"queries": nq, "seconds": sec, "gf_sets_per_s": nq / sec,
+            "network": f"{IN_PAD} -> {layers}x{hidden} GELU -> {NFUND * nt} (bf16, fp32 accumulate), + mixing to "
+                       f"{NCOMP} x {nt}"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm-bench", action="store_true", help="only time ewf_mlp_gemm against cuBLAS")
+    ap.add_argument("--infer-bench", action="store_true", help="only time inference at the study's network size")
     ap.add_argument("--train-runs", type=int, default=256)
     ap.add_argument("--test-runs", type=int, default=64)
     ap.add_argument("--n", type=int, default=192)
@@ -630,6 +666,10 @@ def main():
 
     import torch
 
+    if a.infer_bench:
+        res = infer_benchmark(nt=a.nt)
+        print(json.dumps(res, indent=1))
+        return
     if a.gemm_bench:
         res = gemm_benchmark()
         print(json.dumps(res, indent=1))

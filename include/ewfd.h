@@ -283,11 +283,14 @@ int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk);
  * buffers are caller-owned device memory; bf16 = __nv_bfloat16 stored as 16-bit words; `stream`
  * is a cudaStream_t (NULL = default).  Calls are asynchronous on the stream.
  * ------------------------------------------------------------------------------------------- */
-/* C[M,N] = A[M,K] . B[N,K]^T (+ bias[N]); A, B bf16 row-major; tensor cores, fp32 accumulation.
- * Optional outputs: Cf fp32, Cb bf16, pre (fp32 value before the activation); act 0 = none,
- * 1 = GELU (erf form).  M, N multiples of 128, K a multiple of 32. */
+/* C[M,N] = A[M,K] . B[N,K]^T (+ bias[N]); A, B bf16 row-major, 16-byte aligned; tcgen05 tensor
+ * cores fed by TMA, fp32 accumulation in tensor memory.  Optional outputs: Cf fp32, Cb bf16,
+ * pre (fp32 value before the activation), 16 / 4 / 16-byte aligned; act 0 = none, 1 = GELU (erf
+ * form).  M, N multiples of 128, K a multiple of 32. */
 int ewf_mlp_gemm(const void *A, const void *B, const float *bias, float *Cf, void *Cb, float *pre, int32_t M, int32_t N,
                  int32_t K, int32_t act, void *stream);
+/* Synchronises and reports (then clears) a failed bounded wait of ewf_mlp_gemm. */
+int ewf_mlp_status(void);
 /* bf16 [rows, cols] -> [cols, rows] */
 int ewf_mlp_transpose(const void *in, void *out, int32_t rows, int32_t cols, void *stream);
 /* dx = dy * GELU'(pre), bf16 out */

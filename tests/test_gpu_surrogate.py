@@ -45,6 +45,36 @@ def test_gemm_matches_fp32_reference(cuda_device):
     assert lib.ewf_mlp_gemm(_p(A), _p(B), None, _p(Cf), None, None, 100, 256, 64, 0, None) == -1
 
 
+def test_gemm_shapes_and_status(cuda_device):
+    """The tcgen05 GEMM against an FP64 product of the same bf16 operands over its shape classes:
+    256-wide tiles (N a multiple of 256) and 128-wide ones, a partial last k-stage (K = 32, 96,
+    544: the tensor map's zero fill), many stages, the surrogate's output-layer shape, bias + GELU
+    with every output, and a clean status afterwards."""
+    import torch
+
+    lib = load_library()
+    g = torch.Generator(device="cpu").manual_seed(1)
+    for M, N, K in ((128, 128, 32), (256, 384, 96), (384, 256, 512), (512, 12800, 512), (256, 512, 544),
+                    (128, 640, 2048)):
+        A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+        B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+        bias = torch.randn(N, generator=g).cuda()
+        Cf = torch.empty(M, N, device="cuda")
+        Cb = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
+        pre = torch.empty(M, N, device="cuda")
+        assert lib.ewf_mlp_gemm(_p(A), _p(B), _p(bias), _p(Cf), _p(Cb), _p(pre), M, N, K, 1, None) == 0
+        torch.cuda.synchronize()
+        assert lib.ewf_mlp_status() == 0
+        ref_pre = A.double() @ B.double().T + bias.double()
+        # fp32 accumulation: the relative error grows like sqrt(K) times the fp32 unit roundoff
+        tol = 1e-6 * max(1.0, (K / 256) ** 0.5)
+        err = ((pre.double() - ref_pre).norm() / ref_pre.norm()).item()
+        assert err < tol, (M, N, K, err)
+        ref = torch.nn.functional.gelu(ref_pre)
+        assert (Cf.double() - ref).norm() / ref.norm() < tol
+        assert (Cb.double() - ref).abs().max() <= 0.01 * ref.abs().max()
+
+
 def test_transpose_adam_and_gelu_grad(cuda_device):
     import torch
 
