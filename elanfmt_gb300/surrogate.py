@@ -653,6 +653,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gemm-bench", action="store_true", help="only time ewf_mlp_gemm against cuBLAS")
     ap.add_argument("--infer-bench", action="store_true", help="only time inference at the study's network size")
+    ap.add_argument("--gemm-once", default="", help="M,N,K: three ewf_mlp_gemm launches of one shape (profiling)")
     ap.add_argument("--train-runs", type=int, default=256)
     ap.add_argument("--test-runs", type=int, default=64)
     ap.add_argument("--n", type=int, default=192)
@@ -666,6 +667,20 @@ def main():
 
     import torch
 
+    if a.gemm_once:
+        import ctypes as C
+
+        M, N, K = (int(v) for v in a.gemm_once.split(","))
+        lib = load_library()
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+        Cf = torch.empty(M, N, device="cuda")
+        for _ in range(3):
+            _check(lib.ewf_mlp_gemm(_p(A), _p(B), None, _p(Cf), None, None, M, N, K, 0, None), "ewf_mlp_gemm")
+        torch.cuda.synchronize()
+        _check(lib.ewf_mlp_status(), "ewf_mlp_status")
+        print("ok", M, N, K)
+        return
     if a.infer_bench:
         res = infer_benchmark(nt=a.nt)
         print(json.dumps(res, indent=1))
