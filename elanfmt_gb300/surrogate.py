@@ -99,19 +99,22 @@ class MLP:
             self._ws[M] = w
         return self._ws[M]
 
-    def forward(self, X) -> "torch.Tensor":
-        """X: bf16 [M, sizes[0]] on the GPU; returns the fp32 output [M, sizes[-1]] (workspace)."""
+    def forward(self, X, Y=None, keep_pre: bool = True) -> "torch.Tensor":
+        """X: bf16 [M, sizes[0]] on the GPU; returns the fp32 output [M, sizes[-1]], written into Y
+        when given (contiguous rows, e.g. a row slice of the caller's output), else into the
+        workspace.  keep_pre=False skips the pre-activations (only the backward pass reads them)."""
         M = X.shape[0]
         w = self._work(M)
         st = _stream()
         w["H"][0].copy_(X)
+        Yd = w["Y"] if Y is None else Y
         for l in range(self.nlayers):
             last = l == self.nlayers - 1
             _check(self.lib.ewf_mlp_gemm(_p(w["H"][l]), _p(self.Wb[l]), _p(self.b[l]),
-                                         _p(w["Y"]) if last else None, None if last else _p(w["H"][l + 1]),
-                                         None if last else _p(w["P"][l]), M, self.sizes[l + 1], self.sizes[l],
-                                         0 if last else 1, st), "ewf_mlp_gemm")
-        return w["Y"]
+                                         _p(Yd) if last else None, None if last else _p(w["H"][l + 1]),
+                                         None if (last or not keep_pre) else _p(w["P"][l]), M, self.sizes[l + 1],
+                                         self.sizes[l], 0 if last else 1, st), "ewf_mlp_gemm")
+        return Yd
 
     def loss_grad(self, T) -> "torch.Tensor":
         """MSE against fp32 targets T; dY of the last layer into the workspace; returns the loss."""
@@ -171,17 +174,20 @@ class MLP:
                 losses.append((s, float(loss)))
         return losses
 
-    def predict(self, X, batch: int = 1024):
+    def predict(self, X, batch: int = 8192):
+        """Inference of X [n, sizes[0]] in batches of `batch` rows: full batches write their rows of
+        the output directly; a ragged last batch is padded to 128 rows and copied."""
         torch = self.torch
         n = X.shape[0]
         out = torch.empty(n, self.sizes[-1], device="cuda")
         for a in range(0, n, batch):
             xb = X[a:a + batch]
             m = xb.shape[0]
-            if m % 128:
-                pad = torch.zeros(128 - m % 128, X.shape[1], dtype=X.dtype, device="cuda")
-                xb = torch.cat([xb, pad])
-            y = self.forward(xb)
+            if m % 128 == 0:
+                self.forward(xb, out[a:a + m], keep_pre=False)
+                continue
+            pad = torch.zeros(128 - m % 128, X.shape[1], dtype=X.dtype, device="cuda")
+            y = self.forward(torch.cat([xb, pad]), keep_pre=False)
             out[a:a + m] = y[:m]
         return out
 
