@@ -37,16 +37,19 @@ __device__ __forceinline__ float gelu_grad(float x)
 }
 
 // ---------------------------------------------------------------------------------------------
-// tcgen05 GEMM: C[M,N] = A[M,K] . B[N,K]^T on the 5th-generation tensor cores.  One CTA per
-// 128 x BN tile of C (BN = 256, or 128 when N is not a multiple of 256); the fp32 accumulator
-// lives in tensor memory (128 lanes x BN columns).  Warp roles, 128 threads:
+// tcgen05 GEMM: C[M,N] = A[M,K] . B[N,K]^T on the 5th-generation tensor cores.  Persistent: one
+// CTA per SM walks the 128 x BN tiles of C (BN = 256, or 128 when N is not a multiple of 256).
+// Two fp32 accumulators of 128 lanes x BN columns in tensor memory, so the epilogue of one tile
+// overlaps the MMAs of the next.  Warp roles, 192 threads:
 //   warp 0, one lane: TMA producer -- per k-stage one 2-D bulk tensor copy per operand (128-byte
-//     swizzle, ewf_umma.h) into the free stage, completing on that stage's "full" mbarrier;
-//   warp 1, one lane: MMA issuer -- waits for "full", issues 4 tcgen05.mma (K = 16 each) and
-//     commits them to the stage's "empty" mbarrier (which frees it for the producer), and after
-//     the last stage to "done";
-//   all 4 warps: epilogue -- wait for "done", read the accumulator with tcgen05.ld (warp w: rows
-//     32w .. 32w+31), add the bias, GELU, write the requested outputs.
+//     swizzle, ewf_umma.h) into the next free slot of a 4-stage ring, completing on that slot's
+//     "full" mbarrier; the ring runs on across tiles;
+//   warp 1, one lane: MMA issuer -- waits for a free accumulator ("acc_empty"), then per stage for
+//     "full", issues 4 tcgen05.mma (K = 16 each) and commits them to the slot's "empty" mbarrier
+//     (freeing it for the producer); after the tile's last stage commits "acc_full";
+//   warps 2-5: epilogue -- wait for "acc_full", read the accumulator with tcgen05.ld (warp w owns
+//     TMEM lanes 32 (w % 4) ..), add the bias, GELU, write the requested outputs, release the
+//     accumulator ("acc_empty", one arrival per warp).
 // K beyond the last full stage is read as zeros (the tensor map's out-of-bounds fill), so any K
 // that is a multiple of 8 works.  Every mbarrier wait is bounded: on timeout the wait raises
 // g_umma_err and gives up (the outputs of that launch are then invalid, ewf_mlp_status reports
@@ -115,29 +118,33 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16])
 template <int BN>
 __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
     k_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
-           const float *__restrict__ bias, float *__restrict__ Cf, __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Pre,
-           int M, int N, int K, int act)
+             const float *__restrict__ bias, float *__restrict__ Cf, __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Pre,
+             int M, int N, int K, int act)
 {
     namespace U = ewf_umma;
     constexpr int STAGE = U::a_bytes() + BN * U::ROW_BYTES;
     extern __shared__ uint8_t smem_raw[];
-    __shared__ uint64_t full[U::STAGES], empty[U::STAGES], done;
+    __shared__ uint64_t full[U::STAGES], empty[U::STAGES], acc_full[2], acc_empty[2];
     __shared__ uint32_t s_tmem;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.y * U::BM, n0 = blockIdx.x * BN;
-    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);  // stage tiles on 1024 B
+    uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
+    const int tiles_n = N / BN, tiles = (M / U::BM) * tiles_n;
+    const int nk = (K + U::BK - 1) / U::BK;
 
     if (tid == 0) {
         for (int s = 0; s < U::STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(&done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        __syncwarp();  // the alloc is warp-collective (.sync.aligned)
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)), "r"(BN)
+        __syncwarp();
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)), "r"(2 * BN)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -145,70 +152,90 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = s_tmem;
-    const int nk = (K + U::BK - 1) / U::BK;
+    bool ok = true;
 
-    if (warp == 0 && lane == 0) {  // TMA producer
-        for (int kt = 0; kt < nk; ++kt) {
-            const int s = kt % U::STAGES;
-            if (kt >= U::STAGES && !mbar_wait(&empty[s], ((kt / U::STAGES) - 1) & 1)) break;
-            uint8_t *As = smem + s * STAGE;
-            mbar_expect_tx(&full[s], STAGE);
-            tma_load_2d(As, &mapA, kt * U::BK, m0, &full[s]);
-            tma_load_2d(As + U::a_bytes(), &mapB, kt * U::BK, n0, &full[s]);
+    if (warp == 0) {
+        if (lane == 0) {  // TMA producer: every k-stage of every tile of this CTA, one ring
+            int g = 0;
+            for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+                const int m0 = (t / tiles_n) * U::BM, n0 = (t % tiles_n) * BN;
+                for (int kt = 0; kt < nk; ++kt, ++g) {
+                    const int s = g % U::STAGES;
+                    if (g >= U::STAGES && !mbar_wait(&empty[s], ((g / U::STAGES) - 1) & 1)) { ok = false; break; }
+                    uint8_t *As = smem + s * STAGE;
+                    mbar_expect_tx(&full[s], STAGE);
+                    tma_load_2d(As, &mapA, kt * U::BK, m0, &full[s]);
+                    tma_load_2d(As + U::a_bytes(), &mapB, kt * U::BK, n0, &full[s]);
+                }
+            }
         }
-    } else if (warp == 1 && lane == 0) {  // MMA issuer
-        const uint32_t idesc = U::instr_desc_bf16_f32(U::BM, BN);
-        int kt = 0;
-        for (; kt < nk; ++kt) {
-            const int s = kt % U::STAGES;
-            if (!mbar_wait(&full[s], (kt / U::STAGES) & 1)) break;
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc = U::instr_desc_bf16_f32(U::BM, BN);
+            int g = 0, i = 0;
+            for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
+                const int b = i & 1;
+                if (i >= 2 && !mbar_wait(&acc_empty[b], ((i >> 1) - 1) & 1)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t d = tmem + (uint32_t)(b * BN);
+                for (int kt = 0; kt < nk; ++kt, ++g) {
+                    const int s = g % U::STAGES;
+                    if (!mbar_wait(&full[s], (g / U::STAGES) & 1)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(smem + s * STAGE), b0 = a0 + U::a_bytes();
+                    for (int j = 0; j < U::BK / U::MMA_K; ++j)
+                        umma_bf16(d, U::smem_desc_sw128(a0 + 32 * j), U::smem_desc_sw128(b0 + 32 * j), idesc,
+                                  (kt > 0 || j > 0) ? 1u : 0u);
+                    umma_commit(&empty[s]);
+                }
+                umma_commit(&acc_full[b]);
+            }
+        }
+    } else {  // epilogue warps 2..5: TMEM lane quarter q = warp % 4
+        const int q = warp & 3;
+        int i = 0;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
+            const int b = i & 1;
+            const bool got = mbar_wait(&acc_full[b], (i >> 1) & 1);
             tc_fence_after();
-            const uint32_t a0 = smem_u32(smem + s * STAGE), b0 = a0 + U::a_bytes();
-            for (int j = 0; j < U::BK / U::MMA_K; ++j)
-                umma_bf16(tmem, U::smem_desc_sw128(a0 + 32 * j), U::smem_desc_sw128(b0 + 32 * j), idesc,
-                          (kt > 0 || j > 0) ? 1u : 0u);
-            umma_commit(&empty[s]);
-        }
-        umma_commit(&done);  // tracks every MMA issued before it
-    }
-    __syncwarp();
-    const bool ok = mbar_wait(&done, 0);
-    tc_fence_after();
-
-    // epilogue: warp w owns accumulator lanes (rows) 32w .. 32w + 31
-    const int row = m0 + 32 * warp + lane;
+            const int m0 = (t / tiles_n) * U::BM, n0 = (t % tiles_n) * BN;
+            const int row = m0 + 32 * q + lane;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-        uint32_t v[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-        float x[16];
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN + c0), v);
+                float x[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            x[q] = ok ? __uint_as_float(v[q]) : __int_as_float(0x7fc00000);
-            if (bias) x[q] += bias[n0 + c0 + q];
+                for (int e = 0; e < 16; ++e) {
+                    x[e] = got ? __uint_as_float(v[e]) : __int_as_float(0x7fc00000);
+                    if (bias) x[e] += bias[n0 + c0 + e];
+                }
+                const size_t o = (size_t)row * N + n0 + c0;
+                if (Pre)
+#pragma unroll
+                    for (int e = 0; e < 16; e += 4) *reinterpret_cast<float4 *>(Pre + o + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+                if (act == 1)
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) x[e] = gelu(x[e]);
+                if (Cf)
+#pragma unroll
+                    for (int e = 0; e < 16; e += 4) *reinterpret_cast<float4 *>(Cf + o + e) = make_float4(x[e], x[e + 1], x[e + 2], x[e + 3]);
+                if (Cb)
+#pragma unroll
+                    for (int e = 0; e < 16; e += 2) *reinterpret_cast<__nv_bfloat162 *>(Cb + o + e) = __floats2bfloat162_rn(x[e], x[e + 1]);
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[b])) : "memory");
         }
-        const size_t o = (size_t)row * N + n0 + c0;
-        if (Pre)
-#pragma unroll
-            for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4 *>(Pre + o + q) = make_float4(x[q], x[q + 1], x[q + 2], x[q + 3]);
-        if (act == 1)
-#pragma unroll
-            for (int q = 0; q < 16; ++q) x[q] = gelu(x[q]);
-        if (Cf)
-#pragma unroll
-            for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4 *>(Cf + o + q) = make_float4(x[q], x[q + 1], x[q + 2], x[q + 3]);
-        if (Cb)
-#pragma unroll
-            for (int q = 0; q < 16; q += 2) *reinterpret_cast<__nv_bfloat162 *>(Cb + o + q) = __floats2bfloat162_rn(x[q], x[q + 1]);
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         __syncwarp();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
     }
 }
-
 int check(cudaError_t e, const char *what);
 
 // 2-D tensor map of a K-major bf16 operand [rows, K] with boxes of BK x box_rows and the 128-byte swizzle
@@ -252,8 +279,12 @@ int launch_gemm(const void *A, const void *B, const float *bias, float *Cf, void
     int st = operand_map(&ma, A, M, K, ewf_umma::BM);
     if (st) return st;
     if ((st = operand_map(&mb, B, N, K, BN))) return st;
-    k_gemm<BN><<<dim3(N / BN, M / ewf_umma::BM), ewf_umma::THREADS, smem, stream>>>(
-        ma, mb, bias, Cf, (__nv_bfloat16 *)Cb, pre, M, N, K, act);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (M / ewf_umma::BM) * (N / BN);
+    const int grid = tiles < sms ? tiles : (sms > 0 ? sms : 1);  // one CTA per SM (shared memory bound)
+    k_gemm<BN><<<grid, ewf_umma::THREADS, smem, stream>>>(ma, mb, bias, Cf, (__nv_bfloat16 *)Cb, pre, M, N, K, act);
     return check(cudaGetLastError(), "gemm launch");
 }
 

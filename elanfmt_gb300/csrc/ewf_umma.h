@@ -34,10 +34,11 @@ constexpr int STAGES = 4;
 constexpr int ROW_BYTES = BK * 2;
 constexpr int ATOM_BYTES = 8 * ROW_BYTES;  // 8 rows x 128 B: the swizzle atom, stride-dimension offset
 constexpr int MMA_K = 16;
-constexpr int THREADS = 128;     // warp 0: TMA producer (one lane); warp 1: MMA issuer (one lane); all: epilogue
+constexpr int THREADS = 192;     // warp 0: TMA producer (one lane); warp 1: MMA issuer (one lane); warps 2-5: epilogue
 constexpr int LAYOUT_SW128 = 2;
 
-// Per tile width BN (128 or 256): bytes of a stage and of the whole pipeline; TMEM columns = BN.
+// Per tile width BN (128 or 256): bytes of a stage and of the whole pipeline; TMEM columns = 2 BN
+// (two accumulators).
 EWF_UHD constexpr int a_bytes() { return BM * ROW_BYTES; }
 EWF_UHD constexpr int b_bytes(int bn) { return bn * ROW_BYTES; }
 EWF_UHD constexpr int stage_bytes(int bn) { return a_bytes() + b_bytes(bn); }

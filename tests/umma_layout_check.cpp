@@ -8,7 +8,7 @@
 //      the first row) lies inside its operand tile;
 //   4. the descriptor fields decode back to their inputs (start address, offsets, version,
 //      SWIZZLE_128B) and the instruction descriptor holds M = 128, N = BN, BF16 / BF16 -> F32;
-//   5. the accumulator's BN fp32 columns are a legal tensor-memory allocation.
+//   5. the two accumulators' 2 x BN fp32 columns are a legal tensor-memory allocation.
 // Prints "ok" or the first failure.
 #include <cstdio>
 
@@ -41,7 +41,9 @@ static int check(int bn)
     if (((id >> 13) & 0xF) != 0) return fail("idesc negate / major", id, 0);
     if ((int)((id >> 17) & 0x3F) != bn / 8 || (int)((id >> 24) & 0x1F) != BM / 16) return fail("idesc shape", id, bn);
     if (id & ((1u << 23) | (1u << 29) | 0xFu | (3u << 30) | (1u << 6))) return fail("idesc reserved bits", id, 0);
-    if (bn < 32 || (bn & (bn - 1)) || bn > 512) return fail("tmem columns", bn, 0);
+    const int cols = 2 * bn;
+    if (cols < 32 || (cols & (cols - 1)) || cols > 512) return fail("tmem columns", cols, 0);
+    if (THREADS != 192) return fail("warp roles: 1 producer + 1 MMA + 4 epilogue warps", THREADS, 192);
     return 0;
 }
 
