@@ -6,12 +6,14 @@ of a point moment tensor in a laterally homogeneous medium, which ewf_mlp_combin
 6 elementary moment tensors x 3 velocity components for the query's azimuth
 (mixing_matrices); the other form maps (depth, offset, first and second azimuthal harmonics) to
 the 18 traces directly.  4 hidden layers of 512 GELU units, bf16 weights and activations, fp32
-accumulation (tensor cores), fp32 master weights and Adam.  The forward and backward passes,
+accumulation (tcgen05 tensor cores, accumulators in tensor memory), fp32 master weights and Adam.
+The forward and backward passes,
 the loss gradient, the optimiser and the mixing run in the hand-written kernels of
 csrc/ewf_mlp.cu; torch provides the device buffers, the row gathers that form minibatches, and
 the sum of the per-block loss partials that is logged.
 
     python -m elanfmt_gb300.surrogate [--train-runs 256] [--test-runs 64] [--out report.json]
+    python -m elanfmt_gb300.surrogate --gemm-bench | --infer-bench | --gemm-once M,N,K
 """
 from __future__ import annotations
 
