@@ -73,6 +73,22 @@ def test_gemm_shapes_and_status(cuda_device):
         ref = torch.nn.functional.gelu(ref_pre)
         assert (Cf.double() - ref).norm() / ref.norm() < tol
         assert (Cb.double() - ref).abs().max() <= 0.01 * ref.abs().max()
+    # fp32-only output with two tiles per SM or more: the epilogue stages rows in shared memory and
+    # writes them with TMA stores (both tile widths, bias + GELU applied in the staged path)
+    for M, N, K, act in ((2048, 4864, 96, 1), (8192, 640, 512, 0), (4096, 12800, 512, 1)):
+        A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+        B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+        bias = torch.randn(N, generator=g).cuda()
+        Cf = torch.full((M, N), float("nan"), device="cuda")
+        assert lib.ewf_mlp_gemm(_p(A), _p(B), _p(bias), _p(Cf), None, None, M, N, K, act, None) == 0
+        torch.cuda.synchronize()
+        assert lib.ewf_mlp_status() == 0
+        ref = A.double() @ B.double().T + bias.double()
+        if act:
+            ref = torch.nn.functional.gelu(ref)
+        tol = 1e-6 * max(1.0, (K / 256) ** 0.5)
+        err = ((Cf.double() - ref).norm() / ref.norm()).item()
+        assert err < tol, (M, N, K, err)
 
 
 def test_transpose_adam_and_gelu_grad(cuda_device):
