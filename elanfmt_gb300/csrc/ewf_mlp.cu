@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
             for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
                 const int m0 = (t / tiles_n) * U::BM, n0 = (t % tiles_n) * BN;
                 for (int kt = 0; kt < nk; ++kt, ++g) {
-                    const int s = g % U::STAGES;
-                    if (g >= U::STAGES && !mbar_wait(&empty[s], ((g / U::STAGES) - 1) & 1)) { ok = false; break; }
+                    const int s = U::ring_slot(g);
+                    if (U::ring_needs_free(g) && !mbar_wait(&empty[s], U::ring_free_parity(g))) { ok = false; break; }
                     uint8_t *As = smem + s * STAGE;
                     mbar_expect_tx(&full[s], STAGE);
                     tma_load_2d(As, &mapA, kt * U::BK, m0, &full[s]);
@@ -178,13 +178,13 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
             const uint32_t idesc = U::instr_desc_bf16_f32(U::BM, BN);
             int g = 0, i = 0;
             for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
-                const int b = i & 1;
-                if (i >= 2 && !mbar_wait(&acc_empty[b], ((i >> 1) - 1) & 1)) { ok = false; break; }
+                const int b = U::acc_buf(i);
+                if (U::acc_needs_free(i) && !mbar_wait(&acc_empty[b], U::acc_free_parity(i))) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t d = tmem + (uint32_t)(b * BN);
                 for (int kt = 0; kt < nk; ++kt, ++g) {
-                    const int s = g % U::STAGES;
-                    if (!mbar_wait(&full[s], (g / U::STAGES) & 1)) { ok = false; break; }
+                    const int s = U::ring_slot(g);
+                    if (!mbar_wait(&full[s], U::ring_full_parity(g))) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t a0 = smem_u32(smem + s * STAGE), b0 = a0 + U::a_bytes();
                     for (int j = 0; j < U::BK / U::MMA_K; ++j)
@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
         const int q = warp & 3;
         int i = 0;
         for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
-            const int b = i & 1;
-            const bool got = mbar_wait(&acc_full[b], (i >> 1) & 1);
+            const int b = U::acc_buf(i);
+            const bool got = mbar_wait(&acc_full[b], U::acc_full_parity(i));
             tc_fence_after();
             const int m0 = (t / tiles_n) * U::BM, n0 = (t % tiles_n) * BN;
             const int row = m0 + 32 * q + lane;

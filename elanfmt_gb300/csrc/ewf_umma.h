@@ -74,4 +74,20 @@ EWF_UHD uint32_t mma_read_end(uint32_t start, int rows)
     return start + (uint32_t)(rows / 8 - 1) * ATOM_BYTES + 7 * ROW_BYTES + 32;
 }
 
+// Phase bookkeeping of the GEMM's mbarriers.  An mbarrier wait with parity P returns once the
+// barrier's current phase has a parity other than P, i.e. once the latest completed phase has
+// parity P; a fresh barrier (phase 0 running) therefore lets a parity-1 wait through at once.
+// Stage ring: the g-th k-stage of a CTA (counted across its tiles) uses slot g % STAGES; its
+// "full" completion is that slot's (g / STAGES)-th, its "empty" completion frees the slot for
+// stage g + STAGES.  Accumulators: the i-th tile of a CTA uses buffer i % 2; "acc_full" completes
+// once per tile in that buffer, "acc_empty" once per drained tile.
+EWF_UHD int ring_slot(int g) { return g % STAGES; }
+EWF_UHD uint32_t ring_full_parity(int g) { return (uint32_t)(g / STAGES) & 1u; }          // consumer of stage g
+EWF_UHD bool ring_needs_free(int g) { return g >= STAGES; }                               // producer of stage g waits?
+EWF_UHD uint32_t ring_free_parity(int g) { return (uint32_t)(g / STAGES - 1) & 1u; }     // ... for stage g - STAGES
+EWF_UHD int acc_buf(int i) { return i & 1; }
+EWF_UHD uint32_t acc_full_parity(int i) { return (uint32_t)(i >> 1) & 1u; }              // epilogue of tile i
+EWF_UHD bool acc_needs_free(int i) { return i >= 2; }                                     // MMAs of tile i wait?
+EWF_UHD uint32_t acc_free_parity(int i) { return (uint32_t)((i >> 1) - 1) & 1u; }        // ... for tile i - 2
+
 }  // namespace ewf_umma
