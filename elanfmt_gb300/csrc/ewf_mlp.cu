@@ -13,13 +13,15 @@
 //   ewf_mlp_adam        Adam step on fp32 master weights, refreshing the bf16 copy
 //   ewf_mlp_combine     out[m,o,t] = sum_f R[m,o,f] G[m,f,t]: per-sample mixing of the predicted
 //                       fundamental traces into the 18 moment-tensor x component traces
-// The GEMM requires M, N multiples of 128 and K a multiple of 32 (checked).
+// The GEMM requires M, N multiples of 128 and K a multiple of 32 (checked on the host).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <cstring>
+#include <mutex>
+#include <set>
 
 #include "ewf_umma.h"
 #include "ewfd.h"
@@ -54,12 +56,19 @@ __device__ __forceinline__ float gelu_grad(float x)
 //     accumulator ("acc_empty", one arrival per warp).  When only the fp32 C is wanted and every
 //     SM has two tiles or more, each warp stages 32 rows x 64 columns in shared memory and writes
 //     them with one TMA store (row-contiguous, asynchronous); otherwise every lane stores its row.
-// K beyond the last full stage is read as zeros (the tensor map's out-of-bounds fill), so any K
-// that is a multiple of 8 works.  Every mbarrier wait is bounded: on timeout the wait raises
-// g_umma_err and gives up (the outputs of that launch are then invalid, ewf_mlp_status reports
-// it); the CTA still frees its tensor memory and returns.
+// K beyond the last full stage would be read as zeros (the tensor map's out-of-bounds fill); the
+// host accepts K multiples of 32.  Every mbarrier wait is bounded (g_umma_wait_limit polls): on
+// timeout the wait raises g_umma_err and gives up (the outputs of that launch are then invalid,
+// ewf_mlp_status reports it), and no later wait of the launch waits at all.  Before the CTA frees
+// its tensor memory and returns, the producer waits (again bounded, with a fixed limit) for the
+// last TMA loads it issued and the MMA issuer for every MMA it issued, whether or not a wait
+// gave up.  Test hook (ewf_mlp_test_hold): the MMA issuer of CTA 0 withholds the accumulator-
+// ready signal of one of its tiles, so the epilogue's wait on it runs out.
 // ---------------------------------------------------------------------------------------------
 __device__ int g_umma_err = 0;
+constexpr int kWaitPolls = 1 << 22;
+__device__ int g_umma_wait_limit = kWaitPolls;
+__device__ int g_umma_hold = -1;  // tile (CTA-local index) of CTA 0 whose acc_full is withheld; -1: none
 
 __device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count)
 {
@@ -74,12 +83,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity)
                  : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ bool umma_failed() { return *(volatile int *)&g_umma_err != 0; }
+// Bounded wait; gives up at once when another wait of the launch has already given up.
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity)
 {
-    for (int i = 0; i < (1 << 22); ++i)
+    const int limit = *(volatile int *)&g_umma_wait_limit;
+    for (int i = 0; i < limit; ++i) {
         if (mbar_try_wait(b, parity)) return true;
+        if ((i & 1023) == 1023 && umma_failed()) break;
+    }
     atomicExch(&g_umma_err, 1);
     return false;
+}
+// Wait for asynchronous work this thread issued itself (fixed bound: the work always completes).
+__device__ __forceinline__ void mbar_drain(uint64_t *b, uint32_t parity)
+{
+    for (int i = 0; i < kWaitPolls; ++i)
+        if (mbar_try_wait(b, parity)) return;
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes)
 {
@@ -128,7 +148,7 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
     namespace U = ewf_umma;
     constexpr int STAGE = U::a_bytes() + BN * U::ROW_BYTES;
     extern __shared__ uint8_t smem_raw[];
-    __shared__ uint64_t full[U::STAGES], empty[U::STAGES], acc_full[2], acc_empty[2];
+    __shared__ uint64_t full[U::STAGES], empty[U::STAGES], acc_full[2], acc_empty[2], mma_drain;
     __shared__ uint32_t s_tmem;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     uint8_t *smem = smem_raw + ((1024u - (smem_u32(smem_raw) & 1023u)) & 1023u);
@@ -144,6 +164,7 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
         }
+        mbar_init(&mma_drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -172,10 +193,14 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
                     tma_load_2d(As + U::a_bytes(), &mapB, kt * U::BK, n0, &full[s]);
                 }
             }
+            // the loads issued last into each slot land before the CTA's shared memory goes
+            for (int q = (g > U::STAGES ? g - U::STAGES : 0); q < g; ++q)
+                mbar_drain(&full[U::ring_slot(q)], U::ring_full_parity(q));
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
             const uint32_t idesc = U::instr_desc_bf16_f32(U::BM, BN);
+            const int hold = blockIdx.x == 0 ? *(volatile int *)&g_umma_hold : -1;
             int g = 0, i = 0;
             for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++i) {
                 const int b = U::acc_buf(i);
@@ -192,15 +217,19 @@ __global__ void __launch_bounds__(ewf_umma::THREADS, 1)
                                   (kt > 0 || j > 0) ? 1u : 0u);
                     umma_commit(&empty[s]);
                 }
-                umma_commit(&acc_full[b]);
+                if (!ok) break;
+                if (i != hold) umma_commit(&acc_full[b]);
             }
+            // every MMA issued completes before the tensor memory is freed
+            umma_commit(&mma_drain);
+            mbar_drain(&mma_drain, 0);
         }
     } else {  // epilogue warps 2..5: TMEM lane quarter q = warp % 4
         const int q = warp & 3;
         int i = 0;
         for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++i) {
             const int b = U::acc_buf(i);
-            const bool got = mbar_wait(&acc_full[b], U::acc_full_parity(i));
+            const bool got = !umma_failed() && mbar_wait(&acc_full[b], U::acc_full_parity(i));
             tc_fence_after();
             const int m0 = (t / tiles_n) * U::BM, n0 = (t % tiles_n) * BN;
             const int row = m0 + 32 * q + lane;
@@ -335,23 +364,31 @@ int output_map(CUtensorMap *m, float *C, int M, int N)
 
 constexpr int EPI_STAGE_BYTES = 4 * 32 * 64 * 4;  // four epilogue warps x 32 rows x 64 fp32
 
+// The kernel's shared-memory attribute is a per-device setting: set once per device ordinal.
+template <int BN>
+int gemm_smem_attribute(int dev, int smem_max)
+{
+    static std::mutex mu;
+    static std::set<int> done;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count(dev)) return EWF_OK;
+    const cudaError_t e = cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    if (e != cudaSuccess) return check(e, "gemm smem attribute");
+    done.insert(dev);
+    return EWF_OK;
+}
+
 template <int BN>
 int launch_gemm(const void *A, const void *B, const float *bias, float *Cf, void *Cb, float *pre, int M, int N, int K,
                 int act, cudaStream_t stream)
 {
-    static bool attr = false;
-    const int smem_max = ewf_umma::smem_bytes(BN) + EPI_STAGE_BYTES;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-        if (e != cudaSuccess) return check(e, "gemm smem attribute");
-        attr = true;
-    }
-    alignas(64) CUtensorMap ma, mb, mc;
-    int st = operand_map(&ma, A, M, K, ewf_umma::BM);
-    if (st) return st;
-    if ((st = operand_map(&mb, B, N, K, BN))) return st;
     int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
+    int st = check(cudaGetDevice(&dev), "gemm device");
+    if (st) return st;
+    if ((st = gemm_smem_attribute<BN>(dev, ewf_umma::smem_bytes(BN) + EPI_STAGE_BYTES))) return st;
+    alignas(64) CUtensorMap ma, mb, mc;
+    if ((st = operand_map(&ma, A, M, K, ewf_umma::BM))) return st;
+    if ((st = operand_map(&mb, B, N, K, BN))) return st;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int tiles = (M / ewf_umma::BM) * (N / BN);
     const int grid = tiles < sms ? tiles : (sms > 0 ? sms : 1);  // one CTA per SM (shared memory bound)
@@ -488,6 +525,15 @@ extern "C" int ewf_mlp_status(void)
         return ewf_fail(EWF_ERR_CUDA, "gemm: an mbarrier wait gave up (outputs of that launch are invalid)");
     }
     return EWF_OK;
+}
+
+extern "C" int ewf_mlp_test_hold(int32_t tile, int32_t polls)
+{
+    const int h = tile >= 0 ? tile : -1;
+    const int v = (tile >= 0 && polls > 0) ? polls : kWaitPolls;
+    int st = check(cudaMemcpyToSymbol(g_umma_wait_limit, &v, sizeof(int)), "gemm wait limit");
+    if (!st) st = check(cudaMemcpyToSymbol(g_umma_hold, &h, sizeof(int)), "gemm hold");
+    return st;
 }
 
 extern "C" int ewf_mlp_transpose(const void *in, void *out, int32_t rows, int32_t cols, void *stream)

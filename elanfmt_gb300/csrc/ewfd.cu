@@ -10,7 +10,9 @@
 #include "ewfd_kernels.cuh"
 #include "ewfd_fused.cuh"
 #include "ewfd_wave.cuh"
+#include "ewfd_sweep.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <condition_variable>
 #include <cstdarg>
@@ -179,7 +181,9 @@ struct ewf_handle {
     void *f_alloc[9] = {};
     void *g_alloc[9] = {};  // second state buffer of the fused step
     bool fused = false;
-    int flip = 0;           // fused: the current state is in g_alloc when 1
+    bool sweep = false;     // lockstep sweep step (ewfd_sweep.cuh)
+    bool dbuf = false;      // double-buffered state (one-pass and sweep steps)
+    int flip = 0;           // double-buffered: the current state is in g_alloc when 1
     bool wave = false;      // wavefront step (ewfd_wave.cuh)
     int nsm = 0;            // multiprocessors of the device
     WaveCtl *d_wctl = nullptr;
@@ -192,6 +196,16 @@ struct ewf_handle {
     int src_version = 0;
     int wave_lag_pct = 100;     // lag = ntx + 1 + CTAs * pct / 100 (autotuned)
     int wave_hold = -1;         // diagnostic: stress item whose done flag is withheld
+    SweepCtl *d_sctl = nullptr;           // sweep step: generation, error flag, hold
+    unsigned long long *d_sflags = nullptr;  // progress flag per CTA
+    SweepCta *d_scta = nullptr;           // column range, neighbours and sources per CTA
+    SrcEntry *d_ssrc = nullptr;           // point sources grouped by CTA and plane
+    int sw_cap = 0, sw_src_cap = 0;       // capacities of d_sflags / d_scta and d_ssrc
+    int sw_per_sm = 2;                    // CTAs per multiprocessor (autotuned)
+    int sw_lag = 3;                       // velocity plane = stress plane - lag (autotuned)
+    int sw_ctas = 0, sw_nct = 0;          // the layout built: CTAs, compute threads per CTA
+    int sw_key[3] = {-1, -1, -1};         // (per_sm, src_version, hold) the layout was built for
+    int sw_hold = -1;                     // diagnostic: CTA whose progress is never published
     void *comp_alloc[3] = {};
     void *m_alloc[12] = {};
     bool m_set[12] = {};
@@ -450,6 +464,10 @@ extern "C" void ewf_destroy(ewf_handle *h)
     cudaFree(h->d_wdone);
     cudaFree(h->d_woff);
     cudaFree(h->d_wsrc);
+    cudaFree(h->d_sctl);
+    cudaFree(h->d_sflags);
+    cudaFree(h->d_scta);
+    cudaFree(h->d_ssrc);
     cudaFree(h->d_rec_off);
     cudaFree(h->d_rec_comp);
     cudaFree(h->d_traces);
@@ -473,7 +491,7 @@ static int validate_params(const ewf_params *p)
     if (p->precision < EWF_PREC_F32 || p->precision > EWF_PREC_F64) return ewf_fail(EWF_ERR_ARG, "unknown precision %d", p->precision);
     if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D && p->damping != EWF_DAMP_PERCOMP)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles or per-component weights (damping 0 or 3)");
-    if (p->fused < EWF_STEP_SPLIT || p->fused > EWF_STEP_WAVE) return ewf_fail(EWF_ERR_ARG, "unknown step form %d", p->fused);
+    if (p->fused < EWF_STEP_SPLIT || p->fused > EWF_STEP_SWEEP) return ewf_fail(EWF_ERR_ARG, "unknown step form %d", p->fused);
     if (p->damping == EWF_DAMP_PERCOMP && (p->model != EWF_MODEL_ISO || p->fused == EWF_STEP_FUSED))
         return ewf_fail(EWF_ERR_UNSUPPORTED, "per-component weights: isotropic model, two-kernel or wavefront step");
     if (p->model != EWF_MODEL_ISO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
@@ -522,7 +540,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
     h->kchunk = p->kchunk > 0 ? p->kchunk : 16;
     h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
-    if (p->fused == EWF_STEP_FUSED && (h->gsteps & 1)) h->gsteps += 1;  // fused graphs replay buffer pairs
+    if ((p->fused == EWF_STEP_FUSED || p->fused == EWF_STEP_SWEEP) && (h->gsteps & 1))
+        h->gsteps += 1;  // double-buffered graphs replay buffer pairs
 
 #define CKH(call)                                                                                    \
     do {                                                                                             \
@@ -545,6 +564,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     CKC(cudaEventCreate(&h->ev1));
     h->fused = p->fused == EWF_STEP_FUSED;
     h->wave = p->fused == EWF_STEP_WAVE;
+    h->sweep = p->fused == EWF_STEP_SWEEP;
+    h->dbuf = h->fused || h->sweep;
     CKC(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
     if (h->wave) {
         CKC(cudaMalloc(&h->d_wctl, sizeof(WaveCtl)));
@@ -553,8 +574,20 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     if (p->model == EWF_MODEL_ORTHO && h->esz == 4)
         h->fdiv = ewf_fdiv_verified((float)p->dx) && ewf_fdiv_verified((float)p->dy) && ewf_fdiv_verified((float)p->dz);
     for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
-    if (h->fused)
+    if (h->dbuf)
         for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->g_alloc[q]));
+    if (h->sweep) {
+        int coop = 0;
+        CKC(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
+        if (!coop) {
+            ewf_destroy(h);
+            return ewf_fail(EWF_ERR_UNSUPPORTED, "the sweep step needs cooperative launches");
+        }
+        CKC(cudaMalloc(&h->d_sctl, sizeof(SweepCtl)));
+        CKC(cudaMemsetAsync(h->d_sctl, 0, sizeof(SweepCtl), h->stream));
+        const int nohold = -1;
+        CKC(cudaMemcpyAsync(&h->d_sctl->hold, &nohold, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    }
     if (p->precision == EWF_PREC_F32_KAHAN)
         for (int q = 0; q < 3; ++q) CKH(alloc_box(h, &h->comp_alloc[q]));
     for (int q = 0; q < n_materials(p->model); ++q)
@@ -650,7 +683,7 @@ extern "C" int ewf_set_field(ewf_handle *h, int32_t field, const void *host, siz
         else k_pack<double, double><<<nb, 256, 0, h->stream>>>((double *)dst, (const double *)h->d_stage, ex, ey, ez, sx, sy);
     }
     CK(cudaGetLastError());
-    if (h->fused && field >= EWF_F_VX && field <= EWF_F_SYZ) {
+    if (h->dbuf && field >= EWF_F_VX && field <= EWF_F_SYZ) {
         // both state buffers hold the cells the step never updates
         void *dst2 = boxptr(h, state_alloc(h, 1 - h->flip, field));
         if (h->esz == 4) {
@@ -1072,18 +1105,163 @@ static void wave_entry(const ewf_handle *h, cudaEvent_t *ev, int)
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
-template <int FORM, typename T, int MODEL, int DAMP, bool KAHAN>
-static step_fn entry()
+// The sweep step: column ranges, neighbour ranges and the grouped point sources for the current
+// CTAs-per-multiprocessor setting, checked against the kernel's occupancy (every CTA must be
+// resident at once).  Rebuilt when the setting or the sources change; never during capture.
+static int sweep_prepare(ewf_handle *h, const void *kern)
 {
-    if (FORM == EWF_STEP_FUSED) return fused_entry<T, MODEL, DAMP, KAHAN>;
-    if (FORM == EWF_STEP_WAVE) return wave_entry<T, MODEL, DAMP, KAHAN>;
-    return step_entry<T, MODEL, DAMP, KAHAN>;
+    if (!h->sweep) return EWF_OK;
+    if (h->sw_ctas > 0 && h->sw_key[0] == h->sw_per_sm && h->sw_key[1] == h->src_version) return EWF_OK;
+    const int nx = h->p.nx, ny = h->p.ny, nz = h->p.nz;
+    const long long ncols = (long long)nx * ny;
+    const int maxthr = h->esz == 4 ? SWEEP_MAX_THREADS : SWEEP_MAX_THREADS / 2;
+    long long ctas = (long long)h->sw_per_sm * std::max(1, h->nsm);
+    ctas = std::min(ctas, std::max(1LL, (ncols + 31) / 32));  // at least a warp of columns per CTA
+    const long long len = (ncols + ctas - 1) / ctas;
+    const long long nct = (len + 31) / 32 * 32;
+    if (nct + 32 > maxthr)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: %lld columns over %lld CTAs need %lld threads per CTA (at most %d)",
+                        ncols, ctas, nct + 32, maxthr);
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)nct + 32, 0));
+    if ((long long)occ * h->nsm < ctas)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: %lld CTAs of %lld threads cannot all be resident (%d per SM)", ctas,
+                        nct + 32, occ);
+    CK(cudaStreamSynchronize(h->stream));
+    const int nc = (int)ctas;
+    std::vector<long long> st((size_t)nc + 1);
+    for (int c = 0; c <= nc; ++c) st[(size_t)c] = (long long)c * ncols / nc;
+    auto owner = [&](long long q) { return (int)(std::upper_bound(st.begin(), st.begin() + nc, q) - st.begin()) - 1; };
+    std::vector<SweepCta> t((size_t)nc);
+    for (int c = 0; c < nc; ++c) {
+        SweepCta &x = t[(size_t)c];
+        x.s = (int)st[(size_t)c];
+        x.e = (int)st[(size_t)c + 1];
+        x.lo = owner(std::max(0LL, (long long)x.s - nx));
+        x.hi = owner(std::min(ncols - 1, (long long)x.e - 1 + nx));
+    }
+    // sources: owner of the entry's column (cells past the last row or column go to the owner of
+    // the nearest column: the velocity update never reads them), then by plane, stable
+    const size_t ns = h->h_src.size();
+    std::vector<int> own(ns), plane(ns), idx(ns);
+    for (size_t e = 0; e < ns; ++e) {
+        const SrcEntry &q = h->h_src[e];
+        own[e] = owner((long long)std::min(q.i, nx - 1) + (long long)std::min(q.j, ny - 1) * nx);
+        plane[e] = std::min(q.k, nz - 1);
+        idx[e] = (int)e;
+    }
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
+        return own[(size_t)x] != own[(size_t)y] ? own[(size_t)x] < own[(size_t)y] : plane[(size_t)x] < plane[(size_t)y];
+    });
+    std::vector<SrcEntry> grouped(ns);
+    for (int c = 0; c < nc; ++c) t[(size_t)c].src0 = t[(size_t)c].src1 = 0;
+    for (size_t r = 0; r < ns; ++r) grouped[r] = h->h_src[(size_t)idx[r]];
+    for (int c = 0, r = 0; c < nc; ++c) {
+        t[(size_t)c].src0 = r;
+        while (r < (int)ns && own[(size_t)idx[(size_t)r]] == c) ++r;
+        t[(size_t)c].src1 = r;
+    }
+    if (nc > h->sw_cap) {
+        cudaFree(h->d_sflags);
+        cudaFree(h->d_scta);
+        h->d_sflags = nullptr;
+        h->d_scta = nullptr;
+        h->sw_cap = 0;
+        CK(cudaMalloc(&h->d_sflags, (size_t)nc * sizeof(unsigned long long)));
+        CK(cudaMemset(h->d_sflags, 0, (size_t)nc * sizeof(unsigned long long)));  // below every target
+        CK(cudaMalloc(&h->d_scta, (size_t)nc * sizeof(SweepCta)));
+        h->sw_cap = nc;
+    }
+    if ((int)ns > h->sw_src_cap) {
+        cudaFree(h->d_ssrc);
+        h->d_ssrc = nullptr;
+        h->sw_src_cap = 0;
+        CK(cudaMalloc(&h->d_ssrc, ns * sizeof(SrcEntry)));
+        h->sw_src_cap = (int)ns;
+    }
+    CK(cudaMemcpy(h->d_scta, t.data(), (size_t)nc * sizeof(SweepCta), cudaMemcpyHostToDevice));
+    if (ns) CK(cudaMemcpy(h->d_ssrc, grouped.data(), ns * sizeof(SrcEntry), cudaMemcpyHostToDevice));
+    h->sw_ctas = nc;
+    h->sw_nct = (int)nct;
+    h->sw_key[0] = h->sw_per_sm;
+    h->sw_key[1] = h->src_version;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+// reads and clears the sweep step's error flag (after the stream has been synchronised)
+static int sweep_check(ewf_handle *h)
+{
+    if (!h->sweep) return EWF_OK;
+    int err = 0;
+    CK(cudaMemcpy(&err, &h->d_sctl->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        CK(cudaMemset(&h->d_sctl->err, 0, sizeof(int)));
+        return ewf_fail(EWF_ERR_CUDA, "sweep step: a wait for a neighbouring CTA gave up; the state of this run is invalid");
+    }
+    return EWF_OK;
+}
+
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+static void sweep_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
+{
+    SweepArgs<T> sa;
+    memset(&sa, 0, sizeof(sa));
+    sa.a = make_args<T>(h, parity);
+    const StepArgs<T> out = make_args<T>(h, 1 - parity);
+    for (int q = 0; q < 9; ++q) sa.o[q] = out.f[q];
+    sa.cta = h->d_scta;
+    sa.src = h->d_ssrc;
+    sa.stf = h->d_stf;
+    sa.nstf = (int)h->nstf;
+    sa.it_ptr = h->d_it;
+    sa.order = h->p.src_order;
+    sa.flags = h->d_sflags;
+    sa.ctl = h->d_sctl;
+    sa.lag = h->sw_lag;
+    sa.nct = h->sw_nct;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)h->sw_ctas);
+    cfg.blockDim = dim3((unsigned)h->sw_nct + 32);
+    cfg.stream = h->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;  // every CTA resident at once (they wait on each other)
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (ev) cudaEventRecord(ev[0], h->stream);
+    cudaLaunchKernelEx(&cfg, k_sweep<T, MODEL, DAMP, KAHAN>, sa);
+    if (ev) {
+        cudaEventRecord(ev[1], h->stream);
+        cudaEventRecord(ev[2], h->stream);
+        cudaEventRecord(ev[3], h->stream);
+    }
+    k_record<T><<<1, 256, 0, h->stream>>>(out, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    if (ev) cudaEventRecord(ev[4], h->stream);
+}
+
+// A step form: the host function that launches one step, and (sweep) the kernel whose
+// occupancy bounds the launch.
+struct StepImpl {
+    step_fn fn;
+    const void *kern;
+};
+
+template <int FORM, typename T, int MODEL, int DAMP, bool KAHAN>
+static StepImpl entry()
+{
+    if constexpr (FORM == EWF_STEP_FUSED) return {fused_entry<T, MODEL, DAMP, KAHAN>, nullptr};
+    else if constexpr (FORM == EWF_STEP_WAVE) return {wave_entry<T, MODEL, DAMP, KAHAN>, nullptr};
+    else if constexpr (FORM == EWF_STEP_SWEEP)
+        return {sweep_entry<T, MODEL, DAMP, KAHAN>, (const void *)k_sweep<T, MODEL, DAMP, KAHAN>};
+    else return {step_entry<T, MODEL, DAMP, KAHAN>, nullptr};
 }
 
 // FORM: EWF_STEP_*; the one-pass form exists for models 0 and 1 with 1-D, 3-D or separable
 // damping (validated), the others for every combination
 template <int FORM>
-static step_fn pick_step_t(const ewf_params &p)
+static StepImpl pick_step_t(const ewf_params &p)
 {
     constexpr int F2 = FORM == EWF_STEP_FUSED ? EWF_STEP_SPLIT : FORM;  // forms built for every model
     const bool iso = p.model == EWF_MODEL_ISO;
@@ -1118,11 +1296,27 @@ static step_fn pick_step_t(const ewf_params &p)
     }
 }
 
-static step_fn pick_step(const ewf_handle *h)
+static StepImpl pick_impl(const ewf_handle *h)
 {
     if (h->fused) return pick_step_t<EWF_STEP_FUSED>(h->p);
     if (h->wave) return pick_step_t<EWF_STEP_WAVE>(h->p);
+    if (h->sweep) return pick_step_t<EWF_STEP_SWEEP>(h->p);
     return pick_step_t<EWF_STEP_SPLIT>(h->p);
+}
+static step_fn pick_step(const ewf_handle *h) { return pick_impl(h).fn; }
+
+// everything a step form needs built before its first launch (never during capture)
+static int step_prepare(ewf_handle *h)
+{
+    int st = wave_prepare(h);
+    if (!st) st = sweep_prepare(h, pick_impl(h).kern);
+    return st;
+}
+static int step_check(ewf_handle *h)
+{
+    int st = wave_check(h);
+    if (!st) st = sweep_check(h);
+    return st;
 }
 
 static int inputs_ready(const ewf_handle *h)
@@ -1150,7 +1344,7 @@ static int build_graph(ewf_handle *h, step_fn fn)
     }
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr, h->fused ? (s & 1) : 0);
+    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr, h->dbuf ? (s & 1) : 0);
     const cudaError_t le = cudaGetLastError();
     const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -1177,16 +1371,16 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
         return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
     if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf)
         return ewf_fail(EWF_ERR_ARG, "source time function has %zu samples, need %d", h->nstf, h->it + nsteps);
-    if ((st = wave_prepare(h))) return st;
+    if ((st = step_prepare(h))) return st;
     const step_fn fn = pick_step(h);
-    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + (h->fused ? h->flip : 0);
+    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + (h->dbuf ? h->flip : 0);
     if (use_graph && (h->graph_dirty || !h->gexec)) {
         st = build_graph(h, fn);
         if (st) return st;
     }
     CK(cudaEventRecord(h->ev0, h->stream));
     int done = 0;
-    int parity = h->fused ? h->flip : 0;
+    int parity = h->dbuf ? h->flip : 0;
     if (use_graph && parity) {  // the graph starts from buffer 0: one direct step first
         fn(h, nullptr, parity);
         parity = 0;
@@ -1203,7 +1397,7 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     }
     for (; done < nsteps; ++done) {
         fn(h, nullptr, parity);
-        if (h->fused) parity ^= 1;
+        if (h->dbuf) parity ^= 1;
     }
     h->flip = parity;
     CK(cudaGetLastError());
@@ -1211,7 +1405,7 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1));
     h->it += nsteps;
-    if ((st = wave_check(h))) return st;
+    if ((st = step_check(h))) return st;
     if (h->p.check_finite && h->nrec > 0 && nsteps > 0) {
         // only the samples of this call: columns [it - nsteps, it) of the nrec x nt traces
         const int t0 = h->it - nsteps;
@@ -1233,7 +1427,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     if (st) return st;
     if (h->it + nsteps > h->p.nt) return ewf_fail(EWF_ERR_ARG, "step %d + %d exceeds nt = %d", h->it, nsteps, h->p.nt);
     if (h->nsrc > 0 && (size_t)(h->it + nsteps) > h->nstf) return ewf_fail(EWF_ERR_ARG, "source time function too short");
-    if ((st = wave_prepare(h))) return st;
+    if ((st = step_prepare(h))) return st;
     const step_fn fn = pick_step(h);
     cudaEvent_t ev[5] = {};
     for (auto &e : ev) CK(cudaEventCreate(&e));
@@ -1241,7 +1435,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     int err = EWF_OK;
     for (int s = 0; s < nsteps && !err; ++s) {
         fn(h, ev, h->flip);
-        if (h->fused) h->flip ^= 1;
+        if (h->dbuf) h->flip ^= 1;
         if (cudaEventSynchronize(ev[4]) != cudaSuccess) { err = ewf_fail(EWF_ERR_CUDA, "kernel timing: %s", cudaGetErrorString(cudaGetLastError())); break; }
         for (int q = 0; q < 4; ++q) {
             float ms = 0.f;
@@ -1253,8 +1447,33 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     if (err) return err;
     CK(cudaGetLastError());
     h->it += nsteps;
-    if ((st = wave_check(h))) return st;
+    if ((st = step_check(h))) return st;
     for (int q = 0; q < 4; ++q) out_ms[q] = acc[q] / nsteps;
+    return EWF_OK;
+}
+
+// Device time of `steps` steps from a reset state (one untimed step first); -1 when the current
+// settings cannot run (e.g. a sweep layout whose CTAs cannot all be resident).
+static int time_setting(ewf_handle *h, int steps, float *ms)
+{
+    int st = ewf_reset(h);
+    if (st) return st;
+    if (step_prepare(h)) {
+        *ms = -1.f;
+        return EWF_OK;
+    }
+    const step_fn fn = pick_step(h);
+    fn(h, nullptr, h->flip);  // warm
+    if (h->dbuf) h->flip ^= 1;
+    CK(cudaEventRecord(h->ev0, h->stream));
+    for (int s = 0; s < steps; ++s) {
+        fn(h, nullptr, h->flip);
+        if (h->dbuf) h->flip ^= 1;
+    }
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if ((st = step_check(h))) return st;
+    CK(cudaEventElapsedTime(ms, h->ev0, h->ev1));
     return EWF_OK;
 }
 
@@ -1268,6 +1487,30 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     if (steps < 1) return ewf_fail(EWF_ERR_ARG, "nt too small to tune");
     if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
     float best = 1e30f;
+    if (h->sweep) {
+        // sweep step: CTAs per multiprocessor x the velocity lag
+        int best_m = -1, best_l = h->sw_lag;
+        for (int m = 1; m <= 4; ++m)
+            for (int lag = 2; lag <= 4; ++lag) {
+                h->sw_per_sm = m;
+                h->sw_lag = lag;
+                h->graph_dirty = true;
+                float ms = 0.f;
+                if ((st = time_setting(h, steps, &ms))) return st;
+                if (ms >= 0.f && ms < best) {
+                    best = ms;
+                    best_m = m;
+                    best_l = lag;
+                }
+            }
+        if (best_m < 0) return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: no layout fits this grid");
+        h->sw_per_sm = best_m;
+        h->sw_lag = best_l;
+        h->graph_dirty = true;
+        if ((st = step_prepare(h))) return st;
+        if (kchunk) *kchunk = h->kchunk;
+        return ewf_reset(h);
+    }
     int best_k = h->kchunk, best_lag = h->wave_lag_pct;
     // wavefront step: slabs of 4..16 planes x lag (100000: every stress item before the first velocity item)
     static const int lag_pct[] = {50, 100, 200, 100000};
@@ -1281,22 +1524,9 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
                 h->wave_lag_pct = lag_pct[vi];
                 h->graph_dirty = true;
             }
-            if ((st = ewf_reset(h))) return st;
-            if ((st = wave_prepare(h))) return st;
-            const step_fn fn = pick_step(h);
-            fn(h, nullptr, h->flip);  // warm
-            if (h->fused) h->flip ^= 1;
-            CK(cudaEventRecord(h->ev0, h->stream));
-            for (int s = 0; s < steps; ++s) {
-                fn(h, nullptr, h->flip);
-                if (h->fused) h->flip ^= 1;
-            }
-            CK(cudaEventRecord(h->ev1, h->stream));
-            CK(cudaStreamSynchronize(h->stream));
-            if ((st = wave_check(h))) return st;
             float ms = 0.f;
-            CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
-            if (ms < best) {
+            if ((st = time_setting(h, steps, &ms))) return st;
+            if (ms >= 0.f && ms < best) {
                 best = ms;
                 best_k = h->kchunk;
                 best_lag = h->wave_lag_pct;
@@ -1308,6 +1538,38 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     h->graph_dirty = true;
     if (kchunk) *kchunk = best_k;
     return ewf_reset(h);
+}
+
+extern "C" int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
+    if (ctas_per_sm < 1 || ctas_per_sm > 8) return ewf_fail(EWF_ERR_ARG, "ctas_per_sm must be in [1, 8] (got %d)", ctas_per_sm);
+    if (lag < 2 || lag > 16) return ewf_fail(EWF_ERR_ARG, "lag must be in [2, 16] (got %d)", lag);
+    h->sw_per_sm = ctas_per_sm;
+    h->sw_lag = lag;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *ctas)
+{
+    if (!h || !ctas_per_sm || !lag || !ctas) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
+    *ctas_per_sm = h->sw_per_sm;
+    *lag = h->sw_lag;
+    *ctas = h->sw_ctas;
+    return EWF_OK;
+}
+
+extern "C" int ewf_sweep_hold(ewf_handle *h, int32_t cta)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
+    if (cta < -1) return ewf_fail(EWF_ERR_ARG, "cta must be >= -1");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(&h->d_sctl->hold, &cta, sizeof(int), cudaMemcpyHostToDevice));
+    return EWF_OK;
 }
 
 extern "C" int ewf_set_wave(ewf_handle *h, int32_t lag_pct)
@@ -1341,7 +1603,7 @@ extern "C" int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct)
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
 {
     if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *n = (h->fused || h->wave) ? 2 : 3 + (h->nsrc > 0 ? 1 : 0);
+    *n = (h->fused || h->wave || h->sweep) ? 2 : 3 + (h->nsrc > 0 ? 1 : 0);
     return EWF_OK;
 }
 
@@ -1469,28 +1731,38 @@ extern "C" int ewf_restore(ewf_handle *h, const char *path)
 // ------------------------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_pack_scratch[EWF_NOALLOC_SCRATCH_BYTES];
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_pack_scratch_mu;
-void *g_pack_scratch_addr[kMaxDevices] = {};
-}  // namespace
-
-// Device address of g_pack_scratch on the current device (looked up on first use).
+// Device address of g_pack_scratch on the current device.  Looked up on every call (a host-side
+// query, no stream work), so a context that was torn down and created again -- where the
+// library's device code may sit at a new address -- never sees a stale address.
 static int pack_scratch_address(void **out)
 {
     int dev = -1;
     CK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return ewf_fail(EWF_ERR_UNSUPPORTED, "device ordinal %d >= %d", dev, kMaxDevices);
-    std::lock_guard<std::mutex> lock(g_pack_scratch_mu);
-    if (!g_pack_scratch_addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_pack_scratch);
-        if (e != cudaSuccess || !p)
-            return ewf_fail(EWF_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
-        g_pack_scratch_addr[dev] = p;
-    }
-    *out = g_pack_scratch_addr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_pack_scratch);
+    if (e != cudaSuccess || !p)
+        return ewf_fail(EWF_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
+    *out = p;
     return EWF_OK;
+}
+
+// The allocation that contains device address p (base and size), through the driver's
+// cuMemGetAddressRange, reached by the runtime's entry-point query so the library needs no
+// link against the driver library.  Returns false where the driver does not know p.
+static bool device_allocation_range(const void *p, unsigned long long *base, size_t *size)
+{
+    typedef int (*range_fn)(unsigned long long *, size_t *, unsigned long long);
+    static range_fn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (range_fn)f;
+        cudaGetLastError();
+    });
+    return fn && fn(base, size, (unsigned long long)(uintptr_t)p) == 0;
 }
 
 extern "C" int ewf_pack_field_noalloc(void *dst, int32_t dst_dtype_bytes, int32_t sx, int64_t sy, const void *host,
@@ -1500,13 +1772,37 @@ extern "C" int ewf_pack_field_noalloc(void *dst, int32_t dst_dtype_bytes, int32_
     if ((dst_dtype_bytes != 4 && dst_dtype_bytes != 8) || (host_dtype_bytes != 4 && host_dtype_bytes != 8))
         return ewf_fail(EWF_ERR_ARG, "dtype bytes must be 4 or 8");
     if (ex < 1 || ey < 1 || ez < 1) return ewf_fail(EWF_ERR_ARG, "extent %dx%dx%d", ex, ey, ez);
-    if (sx < ex || sy < (int64_t)sx * ey)
+    if (sx < ex || sy < (int64_t)sx * ey || sy > (int64_t(1) << 40))
         return ewf_fail(EWF_ERR_ARG, "pitches sx=%d sy=%lld do not hold %dx%d rows", sx, (long long)sy, ex, ey);
     const size_t n = (size_t)ex * ey * ez;
     const size_t bytes = n * (size_t)host_dtype_bytes;
     if (bytes > EWF_NOALLOC_SCRATCH_BYTES)
         return ewf_fail(EWF_ERR_ARG, "array of %zu bytes exceeds the %u-byte no-allocation scratch", bytes,
                         (unsigned)EWF_NOALLOC_SCRATCH_BYTES);
+    if ((uintptr_t)dst % (uintptr_t)dst_dtype_bytes != 0)
+        return ewf_fail(EWF_ERR_ARG, "dst %p is not aligned to its %d-byte elements", dst, dst_dtype_bytes);
+    // dst must be device memory of the current device (or managed memory), and the last element
+    // the conversion writes must lie inside dst's allocation: checked here so that a wrong
+    // pointer becomes EWF_ERR_ARG instead of a kernel's out-of-range access
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, dst) != cudaSuccess) {
+        cudaGetLastError();
+        return ewf_fail(EWF_ERR_ARG, "dst %p is not memory the CUDA runtime knows", dst);
+    }
+    if (pa.type == cudaMemoryTypeDevice ? pa.device != dev : pa.type != cudaMemoryTypeManaged)
+        return ewf_fail(EWF_ERR_ARG, "dst %p is not device memory of device %d or managed memory", dst, dev);
+    const unsigned long long last = (unsigned long long)(uintptr_t)dst +
+        ((unsigned long long)(ex - 1) + (unsigned long long)(ey - 1) * (unsigned)sx + (unsigned long long)(ez - 1) * sy +
+         1ull) * (unsigned)dst_dtype_bytes;
+    unsigned long long abase = 0;
+    size_t asize = 0;
+    if (!device_allocation_range(dst, &abase, &asize))
+        return ewf_fail(EWF_ERR_ARG, "dst %p: its allocation range is unknown to the driver", dst);
+    if (last > abase + asize)
+        return ewf_fail(EWF_ERR_ARG, "dst %p: the %dx%dx%d extent with pitches %d, %lld ends %llu bytes past its allocation",
+                        dst, ex, ey, ez, sx, (long long)sy, last - (abase + asize));
     void *scratch = nullptr;
     const int st = pack_scratch_address(&scratch);
     if (st) return st;

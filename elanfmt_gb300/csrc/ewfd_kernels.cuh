@@ -63,13 +63,16 @@ struct SrcEntry {
 template <typename T>
 __device__ __forceinline__ T ld(const T *p) { return __ldg(p); }
 
-// State loads.  COH = false: the read-only path (the field is not written during the launch).
-// COH = true: a plain coherent load, for the wavefront step, where other CTAs of the same
-// launch write the fields (ordered by its release/acquire flags).
-template <bool COH, typename T>
+// State loads.  COH = 0: the read-only path (the field is not written during the launch).
+// COH = 1: a plain coherent load, for the wavefront step, where other CTAs of the same launch
+// write the fields (ordered by its release/acquire flags).  COH = 2: a load cached in L2 only
+// (ld.global.cg), for the sweep step's reads of values other CTAs wrote: no L1 line can hold
+// an older copy.
+template <int COH, typename T>
 __device__ __forceinline__ T lds(const T *p)
 {
-    if constexpr (COH) return *p;
+    if constexpr (COH == 2) return __ldcg(p);
+    else if constexpr (COH == 1) return *p;
     else return __ldg(p);
 }
 
@@ -117,7 +120,7 @@ struct StressIn {
 };
 
 // State part of a cell's stress inputs (c: state index, x stride R).
-template <typename T, int MODEL, int DAMP, int RC, bool COH = false>
+template <typename T, int MODEL, int DAMP, int RC, int COH = 0>
 __device__ __forceinline__ void stress_load_state(const StepArgs<T> &a, long long c, StressIn<T, MODEL, DAMP> &q)
 {
     const int R = RC ? RC : a.R;
@@ -162,7 +165,7 @@ __device__ __forceinline__ void stress_load_mat(const StepArgs<T> &a, long long 
     }
 }
 // c: state index (x stride R), cm: material index of the same cell
-template <typename T, int MODEL, int DAMP, int RC, bool COH = false>
+template <typename T, int MODEL, int DAMP, int RC, int COH = 0>
 __device__ __forceinline__ void stress_load(const StepArgs<T> &a, long long c, long long cm, int k,
                                             StressIn<T, MODEL, DAMP> &q)
 {
@@ -287,7 +290,7 @@ __device__ __forceinline__ void stress_store(const StepArgs<T> &a, long long c, 
 // RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
 // SOFF (with RC = 1): the state lives soff elements after the materials' index (one of several
 // right-hand sides in separate boxes of the same geometry).  COH: coherent state loads (lds).
-template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false, bool COH = false>
+template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false, int COH = 0>
 __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1, long long soff = 0)
 {
     constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices
@@ -385,7 +388,7 @@ struct VelIn {
 
 // State part of a cell's velocity inputs (c: state index, x stride R): the stresses around the
 // cell and the old velocities.
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool COH = false>
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, int COH = 0>
 __device__ __forceinline__ void vel_load_state(const StepArgs<T> &a, long long c, VelIn<T, MODEL, DAMP, KAHAN> &q)
 {
     const int R = RC ? RC : a.R;
@@ -422,7 +425,7 @@ __device__ __forceinline__ void vel_load_mat(const StepArgs<T> &a, long long cm,
         q.w = (DAMP == DAMP_W3D) ? ld(a.w3 + cm) : ld(a.w1[2] + k);
     }
 }
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool COH = false>
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, int COH = 0>
 __device__ __forceinline__ void vel_load(const StepArgs<T> &a, long long c, long long cm, int k,
                                          VelIn<T, MODEL, DAMP, KAHAN> &q)
 {
@@ -516,7 +519,7 @@ __device__ __forceinline__ void vel_store(const StepArgs<T> &a, long long c, int
     }
 }
 
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, bool COH = false>
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, int COH = 0>
 __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0)
 {
     constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices (see stress_column)

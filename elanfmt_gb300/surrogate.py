@@ -160,8 +160,14 @@ class MLP:
                                          self.b[l].numel(), C.c_float(lr), C.c_float(b1), C.c_float(b2), C.c_float(eps),
                                          self.step_count, C.c_float(0.0), st), "adam b")
 
+    def check_status(self) -> None:
+        """Raises if a GEMM launch since the last check gave up on a bounded wait (its outputs, and
+        everything computed from them, are invalid).  Synchronises the device."""
+        _check(self.lib.ewf_mlp_status(), "ewf_mlp_status")
+
     def train(self, X, T, steps: int, batch: int = 256, lr: float = 1e-3, seed: int = 0, log_every: int = 0) -> list:
-        """X: bf16 [n, sizes[0]], T: fp32 [n, sizes[-1]] on the GPU.  Cosine learning-rate decay."""
+        """X: bf16 [n, sizes[0]], T: fp32 [n, sizes[-1]] on the GPU.  Cosine learning-rate decay.
+        The GEMMs' status is checked at every logged step and at the end."""
         torch = self.torch
         n = X.shape[0]
         g = torch.Generator(device="cuda").manual_seed(seed)
@@ -173,7 +179,9 @@ class MLP:
             self.backward(batch)
             self.adam(batch, lr * 0.5 * (1 + math.cos(math.pi * s / steps)))
             if log_every and (s % log_every == 0 or s == steps - 1):
+                self.check_status()
                 losses.append((s, float(loss)))
+        self.check_status()
         return losses
 
     def predict(self, X, batch: int = 8192):
@@ -191,6 +199,7 @@ class MLP:
             pad = torch.zeros(128 - m % 128, X.shape[1], dtype=X.dtype, device="cuda")
             y = self.forward(torch.cat([xb, pad]), keep_pre=False)
             out[a:a + m] = y[:m]
+        self.check_status()
         return out
 
 

@@ -71,9 +71,14 @@ typedef enum ewf_damping {
 typedef enum ewf_step_form {
     EWF_STEP_SPLIT = 0, /* stress kernel, injection, velocity kernel (reference order OK4:485-498) */
     EWF_STEP_FUSED = 1, /* one-pass step kernel, double-buffered state (models 0 and 1) */
-    EWF_STEP_WAVE = 2   /* one persistent launch of the stress and velocity updates over tile x slab
+    EWF_STEP_WAVE = 2,  /* one persistent launch of the stress and velocity updates over tile x slab
                          * items in dependency order, in place: the velocity update reads the new
                          * stresses back from L2 (every model, damping and precision) */
+    EWF_STEP_SWEEP = 3  /* one cooperative launch per step: every CTA resident, each owning a balanced
+                         * range of (i,j) columns, all sweeping z in lockstep -- stress of plane p,
+                         * then velocity of plane p - lag from the neighbours' new stresses in L2;
+                         * double-buffered state, one DRAM pass per step (every model, damping and
+                         * precision; grids up to about 2 x 152 x 736 columns nx*ny in FP32) */
 } ewf_step_form;
 
 typedef enum ewf_src_order {
@@ -116,7 +121,8 @@ typedef struct ewf_params {
     int32_t kchunk;       /* planes per CTA of the z-marching kernels; 0 = autotuned/default */
     int32_t graph_steps;  /* steps captured per CUDA graph; 0 = default, <0 = no graph */
     int32_t check_finite; /* 1: ewf_run checks the receiver traces for NaN/Inf */
-    int32_t fused;        /* ewf_step_form: 0 (default) two kernels; 1 one-pass kernel; 2 wavefront */
+    int32_t fused;        /* ewf_step_form: 0 (default) two kernels; 1 one-pass kernel; 2 wavefront;
+                           * 3 lockstep sweep */
     double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
     double c66;            /* isotropic shear modulus pa2[7] (OK4:405); PERCOMP: the xy one */
     double c44, c55;       /* PERCOMP shear moduli of yz and xz, pa2[5], pa2[6] */
@@ -194,7 +200,8 @@ int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
 
 /* Autotuner: times `nsteps` steps for each z-chunk candidate (planes per CTA) with CUDA events,
  * keeps the fastest (returned in *kchunk, may be NULL) and resets the state.  The wavefront
- * step also tunes its lag (kept in the handle). */
+ * step also tunes its lag (kept in the handle); the sweep step tunes its CTAs per
+ * multiprocessor and its lag instead of the z-chunk. */
 int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
 
 /* Wavefront step (fused = EWF_STEP_WAVE): the lag of the velocity items behind the stress items
@@ -207,6 +214,18 @@ int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct);
  * wait and ewf_run returns EWF_ERR_CUDA (the state of that run is invalid; the handle stays
  * usable after ewf_reset).  -1 restores normal operation. */
 int ewf_wave_hold(ewf_handle *h, int32_t item);
+
+/* Sweep step (fused = EWF_STEP_SWEEP): CTAs per multiprocessor (1..8; all CTAs must fit at once)
+ * and the lag of the velocity plane behind the stress plane (2..16), both set by ewf_autotune;
+ * results do not depend on them.  ewf_get_sweep also returns the CTAs of the layout last built
+ * (0 before the first run).  EWF_ERR_STATE for the other step forms. */
+int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag);
+int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *ctas);
+/* Diagnostic for tests of the failure path: CTA `cta` of the sweep step never publishes its
+ * progress, so its neighbours give up after their bounded wait and ewf_run returns EWF_ERR_CUDA
+ * (the state of that run is invalid; the handle stays usable after ewf_reset).  -1 restores
+ * normal operation. */
+int ewf_sweep_hold(ewf_handle *h, int32_t cta);
 
 /* Writes 0_infos.inf and 0_0_{Src,Rec,Rec_x,Rec_y,Rec_y2,Vx,Vy,Vz}.res into workdir
  * (OK4:521-532).  Rec* are the first four receivers. */
@@ -236,8 +255,12 @@ int ewf_snapshot_wait(ewf_handle *h);
  * holds it until exit); arrays larger than that are rejected with EWF_ERR_ARG.  It calls no
  * cudaMalloc/cudaFree.  `stream` is a cudaStream_t (NULL = the default stream); the call
  * returns once the copy is complete.
- *   - The first call on a device looks up the scratch's device address on that device (with
- *     it current); make that first call before any stream capture.
+ *   - dst must be device memory of the current device (or managed memory), aligned to
+ *     dst_dtype_bytes, and the extent at the given pitches must end inside dst's allocation;
+ *     anything else is rejected with EWF_ERR_ARG before any device work.
+ *   - Each call looks up the scratch's device address on the current device (a host-side
+ *     query; it stays valid after a device reset).  The first call on a device also loads the
+ *     library's device code there: make that first call before any stream capture.
  *   - All calls share the one scratch array: calls that overlap on the GPU (from several host
  *     threads or streams) race.  Only dst's cells inside the extent are written.
  */
@@ -291,6 +314,12 @@ int ewf_mlp_gemm(const void *A, const void *B, const float *bias, float *Cf, voi
                  int32_t K, int32_t act, void *stream);
 /* Synchronises and reports (then clears) a failed bounded wait of ewf_mlp_gemm. */
 int ewf_mlp_status(void);
+/* Test hook of the failure path: with tile >= 0, the MMA issuer of the first CTA of every later
+ * ewf_mlp_gemm launch withholds the accumulator-ready signal of its tile number `tile` (a signal
+ * nothing else gives), and every mbarrier wait gives up after `polls` polls; the epilogue's wait
+ * on that tile runs out, the launch still ends and ewf_mlp_status reports it.  tile < 0 restores
+ * normal operation (default limit 2^22 polls). */
+int ewf_mlp_test_hold(int32_t tile, int32_t polls);
 /* bf16 [rows, cols] -> [cols, rows] */
 int ewf_mlp_transpose(const void *in, void *out, int32_t rows, int32_t cols, void *stream);
 /* dx = dy * GELU'(pre), bf16 out */

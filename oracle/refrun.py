@@ -72,6 +72,24 @@ def available(model: int = F.MODEL_ISO, variant: str = "exact", vdamp: float = 0
     return os.path.exists(cubin(model, variant, vdamp, damping))
 
 
+def trace_errors(ours: np.ndarray, ref: np.ndarray) -> dict:
+    """Relative L2 error of each trace of `ours` against `ref` (traces x samples).  Traces whose
+    reference is identically zero are counted apart: `ours` must be zero there too."""
+    ours = np.asarray(ours, np.float64)
+    ref = np.asarray(ref, np.float64)
+    assert ours.shape == ref.shape, (ours.shape, ref.shape)
+    rel, zero_mismatch = [], 0
+    for a, b in zip(ours, ref):
+        nb = float(np.linalg.norm(b))
+        if nb == 0.0:
+            zero_mismatch += int(np.linalg.norm(a) != 0.0)
+            continue
+        rel.append(float(np.linalg.norm(a - b)) / nb)
+    rel = np.array(rel) if rel else np.zeros(1)
+    return {"max_rel_l2": float(rel.max()), "median_rel_l2": float(np.median(rel)),
+            "p90_rel_l2": float(np.percentile(rel, 90)), "traces": int(len(ref)), "zero_mismatch": zero_mismatch}
+
+
 class _Args:
     """Kernel argument vector: ('p', ptr) | ('f', float32) | ('i', int32)."""
 
@@ -123,14 +141,19 @@ class RefRunner:
         self.src = self._upload(np.asarray(m.stf[: m.nt], np.float32)) if m.stf is not None else self._alloc((m.nt,))
         nrec = 0 if m.receivers is None else len(m.receivers)
         self.traces = np.zeros((nrec, m.nt), np.float64)
+        # receivers grouped by field: one index_select per field and step into a device trace
+        # buffer, copied to the host when a run() ends
+        self._dtraces = torch.zeros((nrec, m.nt), dtype=torch.float64, device=self.dev) if nrec else None
+        self._rec_groups = []
         if nrec:
-            offs, comps = [], []
-            for i, j, k, c in m.receivers:
+            by_comp = {}
+            for r, (i, j, k, c) in enumerate(m.receivers):
                 ez, ey, ex = F.shape(int(c), nx, ny, nz)
-                offs.append(int(i) + ex * (int(j) + ey * int(k)))
-                comps.append(int(c))
-            self.rec_off = torch.tensor(offs, device=self.dev)
-            self.rec_comp = comps
+                by_comp.setdefault(int(c), []).append((r, int(i) + ex * (int(j) + ey * int(k))))
+            for c, lst in sorted(by_comp.items()):
+                rows = torch.tensor([r for r, _ in lst], device=self.dev)
+                offs = torch.tensor([o for _, o in lst], device=self.dev)
+                self._rec_groups.append((c, rows, offs))
         self.it = 0
         self._setup_kernels()
 
@@ -347,11 +370,12 @@ class RefRunner:
                 self.a_vel.set_int(self.it_pos_vel, it)
             self._launch(self.k_vel, self.a_vel)
             _ck(lib().refk_sync(), "sync")
-            if len(self.traces):
-                vals = [self.f[c][int(o)] for c, o in zip(self.rec_comp, self.rec_off.tolist())]
-                self.traces[:, it] = torch.stack(vals).double().cpu().numpy()
+            for c, rows, offs in self._rec_groups:
+                self._dtraces[rows, it] = self.f[c].index_select(0, offs).double()
             self.it += 1
         torch.cuda.synchronize()
+        if self._dtraces is not None:
+            self.traces = self._dtraces.cpu().numpy()
 
     def fields(self) -> list[np.ndarray]:
         m = self.m

@@ -91,6 +91,33 @@ def test_gemm_shapes_and_status(cuda_device):
         assert err < tol, (M, N, K, err)
 
 
+def test_gemm_wait_gives_up_and_next_launch_recovers(cuda_device):
+    """Failure path of the GEMM's bounded waits: the test hook withholds the accumulator-ready
+    signal of the first CTA's first tile (a signal nothing else gives), so the epilogue's wait
+    runs out; the launch still ends, ewf_mlp_status reports it, and the next launch is exact."""
+    import torch
+
+    lib = load_library()
+    g = torch.Generator(device="cpu").manual_seed(3)
+    M, N, K = 256, 512, 128
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    Cf = torch.zeros(M, N, device="cuda")
+    assert lib.ewf_mlp_status() == 0
+    assert lib.ewf_mlp_test_hold(0, 20000) == 0
+    try:
+        assert lib.ewf_mlp_gemm(_p(A), _p(B), None, _p(Cf), None, None, M, N, K, 0, None) == 0
+        st = lib.ewf_mlp_status()
+    finally:
+        assert lib.ewf_mlp_test_hold(-1, 0) == 0
+    assert st == -2 and b"gave up" in lib.ewf_last_error()
+    assert torch.isnan(Cf[:128, :256]).all(), "the held tile's outputs are marked invalid"
+    assert lib.ewf_mlp_gemm(_p(A), _p(B), None, _p(Cf), None, None, M, N, K, 0, None) == 0
+    assert lib.ewf_mlp_status() == 0
+    ref = A.double() @ B.double().T
+    assert (Cf.double() - ref).norm() / ref.norm() < 1e-6
+
+
 def test_transpose_adam_and_gelu_grad(cuda_device):
     import torch
 
