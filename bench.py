@@ -57,8 +57,9 @@ def parse():
     ap.add_argument("--size", type=str, default="", help="override grid, e.g. 128x128x96 (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, cpu baseline, reference_gpu, kernel timing")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--step", default="split", choices=["split", "fused", "wave"],
-                    help="step form: two kernels (default), the one-pass kernel, or the wavefront launch")
+    ap.add_argument("--step", default="split", choices=["split", "fused", "wave", "sweep"],
+                    help="step form: two kernels (default), the one-pass kernel, the wavefront launch or the "
+                         "lockstep sweep")
     ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
     ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
     return ap.parse_args()
@@ -252,6 +253,95 @@ def parity_vs_reference(m, form: int) -> dict | None:
                   "full run, same inputs" + (" (the ANISO built-in moment tensor)" if m.model == F.MODEL_ORTHO else "")}
 
 
+def extra_iso(form: int) -> dict:
+    """Isotropic homogeneous 128^3, 1000 steps, 8-receiver ring (the plain isotropic workload):
+    Gcell-updates/s over full runs with the autotuned setting, the step roofline, and full-run
+    seismogram parity against the reference's stock build."""
+    from elanfmt_gb300.solver import Solver
+
+    m, desc = workload("iso", 0, "")
+    with Solver.from_model(m, fused=form) as s:
+        s.autotune(20)
+        s.reset()
+        s.run(m.nt)
+        ms = []
+        for _ in range(3):
+            s.reset()
+            ms.append(s.run(m.nt))
+    best = statistics.median(ms)
+    value = m.cells * m.nt / (best * 1e-3) / 1e9
+    peak, kind = peaks()
+    return {"workload": desc, "value": round(value, 3), "unit": UNIT, "ms_per_run": round(best, 3), "runs": len(ms),
+            "step_roofline": {"bytes_per_cell": STEP_BYTES["iso"], "achieved": round(value * STEP_BYTES["iso"], 1),
+                              "peak": peak, "unit": "GB/s", "frac": round(value * STEP_BYTES["iso"] / peak, 4),
+                              "peak_kind": kind},
+            "parity": parity_vs_reference(m, form)}
+
+
+def extra_batch(nt: int = 300) -> dict:
+    """The batched workload (6 elementary moment tensors on an orthorhombic 256^3 model + 16
+    isotropic models 96^3-224^3) on a shortened run of `nt` steps: runs/s of the batched launch
+    against each solve launched alone, both on the same steps."""
+    from elanfmt_gb300.solver import Batch, Solver
+
+    probs = batch_workload(nt)
+    runs = sum(len(r) for _, r in probs)
+    with Batch(probs) as b:
+        b.autotune(5)
+        b.run(nt)
+        b.reset()
+        batch_s = b.run(nt) * 1e-3
+    solo_s = 0.0
+    for m, rl in probs:
+        for ent, coef in rl:
+            with Solver.from_model(m) as s:
+                s.set_sources(ent, coef)
+                s.run(min(10, nt))
+                s.reset()
+                solo_s += s.run(nt) * 1e-3
+    return {"workload": f"6 elementary MTs on orthorhombic 256^3 + 16 isotropic models 96^3-224^3, {nt} steps "
+                        f"(the full workload runs 3000)", "runs": runs, "batched_runs_per_s": round(runs / batch_s, 3),
+            "solo_runs_per_s": round(runs / solo_s, 3), "speedup_vs_solo": round(solo_s / batch_s, 3)}
+
+
+def extra_surrogate() -> dict:
+    """The learned Green's-function surrogate at the study's network size: inference GF sets/s
+    (CUDA events, 4096 queries, forward pass + azimuthal mixing, 1024 samples) next to the
+    solver's GF sets/s on the surrogate's 192^3 grid (one source, its 6 elementary runs batched,
+    every surface receiver of the study's 12-cell mesh, a 128-step sample scaled to 1024 steps);
+    the held-out error is the committed study's."""
+    import numpy as np
+
+    from elanfmt_gb300 import fields as F
+    from elanfmt_gb300 import surrogate as SG
+    from elanfmt_gb300.solver import Batch
+
+    inf = SG.infer_benchmark(nq=4096, nt=1024)
+    m = SG.layered_iso(n=192, nt=1024)
+    rec_xy = SG.surface_receivers(192, 15, 6)
+    rec = np.array([(i, j, 1, c) for i, j in rec_xy for c in (0, 1, 2)], np.int32)
+    m.receivers = rec
+    rl = []
+    for q in range(6):
+        mt = np.zeros(6)
+        mt[q] = 1.0
+        rl.append(F.mt_point_entries(mt, 96, 96, 40))
+    sample = 128
+    with Batch([(m, rl)]) as b:
+        b.run(sample)
+        b.reset()
+        s_per_src = b.run(sample) * 1e-3 * (1024 / sample)
+    fdtd = len(rec_xy) / s_per_src
+    out = {"network": inf["network"], "surrogate_gf_sets_per_s": round(inf["gf_sets_per_s"], 1),
+           "fdtd_gf_sets_per_s": round(fdtd, 1), "ratio": round(inf["gf_sets_per_s"] / fdtd, 1),
+           "fdtd_sample": f"{sample} of 1024 steps, 192^3, 6 RHS batched, {len(rec_xy)} receivers, scaled linearly"}
+    study = os.path.join(ROOT, "profiles", "surrogate_study.json")
+    if os.path.exists(study):
+        res = json.load(open(study))
+        out["held_out_error"] = {k: res.get(k) for k in ("median_rel_l2", "p90_rel_l2", "served_at_1e-3", "workload")}
+    return out
+
+
 def main():
     args = parse()
     import torch
@@ -278,7 +368,7 @@ def main():
     torch.cuda.set_device(local)
     m, desc = workload(args.workload, args.nt, args.size)
     nt = m.nt
-    form = {"split": F.STEP_SPLIT, "fused": F.STEP_FUSED, "wave": F.STEP_WAVE}[args.step]
+    form = {"split": F.STEP_SPLIT, "fused": F.STEP_FUSED, "wave": F.STEP_WAVE, "sweep": F.STEP_SWEEP}[args.step]
     s = Solver.from_model(m, fused=form, kchunk=args.kchunk)
     # the library's autotuner (z-chunk; the wavefront lag too) unless both are given
     kchunk = args.kchunk if args.kchunk and (form != F.STEP_WAVE or args.wave_lag) else s.autotune(30)
@@ -312,6 +402,8 @@ def main():
         "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": nt, "receivers": len(m.receivers),
                    "kchunk_autotuned": kchunk, "step": args.step,
                    **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {}),
+                   **({"sweep_layout": dict(zip(("ctas_per_sm", "lag", "l2_prefetch", "ctas"), s.sweep_layout()))}
+                      if form == F.STEP_SWEEP else {}),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (working set ~%.1f GB)" % (m.cells * 4 * 21 / 1e9)},
         "gpu_launches": launches,
@@ -331,7 +423,7 @@ def main():
             names = {"stress": "k_stress", "velocity": "k_velocity"}
         else:  # one kernel does the whole step: its compulsory bytes are the one-pass step's
             kb = {"stress": STEP_BYTES[args.workload]}
-            names = {"stress": "k_wave" if form == F.STEP_WAVE else "k_step"}
+            names = {"stress": {F.STEP_WAVE: "k_wave", F.STEP_SWEEP: "k_sweep"}.get(form, "k_step")}
         kernels = {}
         for k in kb:
             achieved = kb[k] * m.cells / (kt[k] * 1e-3) / 1e9
@@ -350,6 +442,15 @@ def main():
     s.close()
     if not args.no_extras and rank == 0:
         out["parity"] = parity_vs_reference(m, form)
+        if args.workload == "ortho" and not args.size and not args.nt:
+            # the other workloads, bounded (about a minute together)
+            for key, fn in (("iso", lambda: extra_iso(form)), ("batch", extra_batch), ("surrogate", extra_surrogate)):
+                t = time.perf_counter()
+                try:
+                    out[key] = fn()
+                except Exception as e:  # an extra leg never voids the headline line
+                    out[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
+                out[key]["bench_seconds"] = round(time.perf_counter() - t, 1)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist:

@@ -2,9 +2,10 @@
 
 Compiles in-tree (outputs next to this file) with nvcc/gcc directly: a few translation units
 built in parallel, one ``-gencode`` for GB300.  The device code is compiled with
-``--fmad=false`` so that every floating-point operation rounds on its own, as in the
-reference's expression order; the kernels are bandwidth-bound, so the separate multiply and
-add cost nothing measurable.
+``--fmad=false`` (host code: ``-ffp-contract=off``) so that every floating-point operation
+rounds on its own, as in the reference's expression order, and host and device code that
+share arithmetic agree bit for bit on both x86 and Arm hosts; the kernels are
+bandwidth-bound, so the separate multiply and add cost nothing measurable.
 """
 from __future__ import annotations
 
@@ -21,7 +22,8 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I", INCLUDE, "-I", CSRC]
 
 LIB = os.path.join(PKG, "libewfd.so")
 EXE = os.path.join(PKG, "ewfd")
@@ -61,7 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
     units = [("ewfd.cu", "ewfd.o"), ("ewfd_batch.cu", "ewfd_batch.o"), ("ewf_mlp.cu", "ewf_mlp.o"),
-             ("ewfd_legacy.cpp", "ewfd_legacy.o")]
+             ("ewfd_post.cu", "ewfd_post.o"), ("ewfd_legacy.cpp", "ewfd_legacy.o")]
     cmds = []
     for src, obj in units:
         extra = ["-x", "cu"] if src.endswith(".cu") else []

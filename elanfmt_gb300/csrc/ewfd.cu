@@ -81,6 +81,8 @@ extern "C" void ewf_params_default(ewf_params *p)
     p->src_order = EWF_SRC_BEFORE_BC1;
     p->check_finite = 1;
     p->fused = 0;
+    p->free_surface = EWF_FS_BC1;
+    p->surface_mu = 0.0;
     p->dx = p->dy = p->dz = 1.0;
     p->dt = 1.0;
 }
@@ -202,7 +204,8 @@ struct ewf_handle {
     SrcEntry *d_ssrc = nullptr;           // point sources grouped by CTA and plane
     int sw_cap = 0, sw_src_cap = 0;       // capacities of d_sflags / d_scta and d_ssrc
     int sw_per_sm = 2;                    // CTAs per multiprocessor (autotuned)
-    int sw_lag = 3;                       // velocity plane = stress plane - lag (autotuned)
+    int sw_pfd = 4;                       // L2 prefetch distance in planes, 0 = off (autotuned)
+    int sw_lag = 4;                       // velocity plane = stress plane - lag - 1 (autotuned, >= 3)
     int sw_ctas = 0, sw_nct = 0;          // the layout built: CTAs, compute threads per CTA
     int sw_key[3] = {-1, -1, -1};         // (per_sm, src_version, hold) the layout was built for
     int sw_hold = -1;                     // diagnostic: CTA whose progress is never published
@@ -373,6 +376,9 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     a.third = (T)1.0 / (T)3.0;
     a.fdiv = h->fdiv ? 1 : 0;
     a.vdamp = (T)h->p.vdamp;
+    a.bc1 = h->p.free_surface == EWF_FS_BC1 ? 1 : 0;
+    a.smu_on = h->p.surface_mu > 0.0 ? 1 : 0;
+    a.smu = (T)h->p.surface_mu;
     return a;
 }
 
@@ -510,6 +516,14 @@ static int validate_params(const ewf_params *p)
                         "plane while other threads read it (a race); no defined result to reproduce");
     if (!(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->dt > 0)) return ewf_fail(EWF_ERR_ARG, "dx, dy, dz, dt must be > 0");
     if (p->kchunk != 0 && p->kchunk < 4) return ewf_fail(EWF_ERR_ARG, "kchunk must be 0 or >= 4");
+    if (p->free_surface != EWF_FS_BC1 && p->free_surface != EWF_FS_NONE)
+        return ewf_fail(EWF_ERR_ARG, "unknown free_surface %d", p->free_surface);
+    if (!(p->surface_mu >= 0.0)) return ewf_fail(EWF_ERR_ARG, "surface_mu must be >= 0");
+    if (p->surface_mu > 0.0 && (p->model != EWF_MODEL_ISO || p->damping != EWF_DAMP_PML1D))
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "surface_mu applies to the isotropic scheme with 1-D PML profiles "
+                                             "(the other schemes take the layer in their edge shear-modulus fields)");
+    if ((p->free_surface != EWF_FS_BC1 || p->surface_mu > 0.0) && p->fused == EWF_STEP_FUSED)
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "the one-pass step applies BC1 and the plain shear modulus only");
     return EWF_OK;
 }
 
@@ -1147,7 +1161,7 @@ static int sweep_prepare(ewf_handle *h, const void *kern)
     for (size_t e = 0; e < ns; ++e) {
         const SrcEntry &q = h->h_src[e];
         own[e] = owner((long long)std::min(q.i, nx - 1) + (long long)std::min(q.j, ny - 1) * nx);
-        plane[e] = std::min(q.k, nz - 1);
+        plane[e] = sweep_src_plane(q, nz);
         idx[e] = (int)e;
     }
     std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
@@ -1220,6 +1234,19 @@ static void sweep_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
     sa.ctl = h->d_sctl;
     sa.lag = h->sw_lag;
     sa.nct = h->sw_nct;
+    // the arrays the control warp prefetches into L2: step n's state, materials, 3-D weights,
+    // the compensation of the compensated form
+    sa.pfd = h->sw_pfd;
+    sa.esz = (int)sizeof(T);
+    auto add_pf = [&](const void *p) {
+        if (p && sa.npf < SWEEP_MAX_PF) sa.pf[sa.npf++] = (const char *)p;
+    };
+    for (int q = 0; q < 9; ++q) add_pf(sa.a.f[q]);
+    for (int q = 0; q < 12; ++q) add_pf(sa.a.m[q]);
+    add_pf(sa.a.w3);
+    for (int q = 0; q < 6; ++q) add_pf(sa.a.w6[q]);
+    if (KAHAN)
+        for (int q = 0; q < 3; ++q) add_pf(sa.a.comp[q]);
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
     cfg.gridDim = dim3((unsigned)h->sw_ctas);
@@ -1374,19 +1401,26 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     if ((st = step_prepare(h))) return st;
     const step_fn fn = pick_step(h);
     const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + (h->dbuf ? h->flip : 0);
-    if (use_graph && (h->graph_dirty || !h->gexec)) {
+    bool graph = use_graph;
+    if (graph && (h->graph_dirty || !h->gexec)) {
         st = build_graph(h, fn);
-        if (st) return st;
+        if (st && h->sweep) {  // a driver that cannot capture the cooperative launch: launch directly
+            cudaGetLastError();
+            h->gsteps = 0;
+            graph = false;
+        } else if (st) {
+            return st;
+        }
     }
     CK(cudaEventRecord(h->ev0, h->stream));
     int done = 0;
     int parity = h->dbuf ? h->flip : 0;
-    if (use_graph && parity) {  // the graph starts from buffer 0: one direct step first
+    if (graph && parity) {  // the graph starts from buffer 0: one direct step first
         fn(h, nullptr, parity);
         parity = 0;
         ++done;
     }
-    if (use_graph) {
+    if (graph) {
         for (; done + h->gsteps <= nsteps; done += h->gsteps) {
             CK(cudaGraphLaunch(h->gexec, h->stream));
             if (h->p.nout > 0 && ((h->it + done) / h->p.nout) != ((h->it + done + h->gsteps) / h->p.nout)) {
@@ -1488,24 +1522,29 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
     float best = 1e30f;
     if (h->sweep) {
-        // sweep step: CTAs per multiprocessor x the velocity lag
-        int best_m = -1, best_l = h->sw_lag;
+        // sweep step: CTAs per multiprocessor x the velocity lag x the L2 prefetch distance
+        int best_m = -1, best_l = h->sw_lag, best_pf = h->sw_pfd;
+        static const int pfd_cand[] = {0, 2, 4, 6};
         for (int m = 1; m <= 4; ++m)
-            for (int lag = 2; lag <= 4; ++lag) {
-                h->sw_per_sm = m;
-                h->sw_lag = lag;
-                h->graph_dirty = true;
-                float ms = 0.f;
-                if ((st = time_setting(h, steps, &ms))) return st;
-                if (ms >= 0.f && ms < best) {
-                    best = ms;
-                    best_m = m;
-                    best_l = lag;
+            for (int lag = 3; lag <= 5; ++lag)
+                for (int pf : pfd_cand) {
+                    h->sw_per_sm = m;
+                    h->sw_lag = lag;
+                    h->sw_pfd = pf;
+                    h->graph_dirty = true;
+                    float ms = 0.f;
+                    if ((st = time_setting(h, steps, &ms))) return st;
+                    if (ms >= 0.f && ms < best) {
+                        best = ms;
+                        best_m = m;
+                        best_l = lag;
+                        best_pf = pf;
+                    }
                 }
-            }
         if (best_m < 0) return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: no layout fits this grid");
         h->sw_per_sm = best_m;
         h->sw_lag = best_l;
+        h->sw_pfd = best_pf;
         h->graph_dirty = true;
         if ((st = step_prepare(h))) return st;
         if (kchunk) *kchunk = h->kchunk;
@@ -1540,24 +1579,28 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     return ewf_reset(h);
 }
 
-extern "C" int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag)
+extern "C" int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag, int32_t prefetch)
 {
     if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
     if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
     if (ctas_per_sm < 1 || ctas_per_sm > 8) return ewf_fail(EWF_ERR_ARG, "ctas_per_sm must be in [1, 8] (got %d)", ctas_per_sm);
-    if (lag < 2 || lag > 16) return ewf_fail(EWF_ERR_ARG, "lag must be in [2, 16] (got %d)", lag);
+    if (lag < SWEEP_GRANT + 1 || lag > 16)
+        return ewf_fail(EWF_ERR_ARG, "lag must be in [%d, 16] (got %d)", SWEEP_GRANT + 1, lag);
+    if (prefetch < 0 || prefetch > 32) return ewf_fail(EWF_ERR_ARG, "prefetch must be in [0, 32] (got %d)", prefetch);
     h->sw_per_sm = ctas_per_sm;
     h->sw_lag = lag;
+    h->sw_pfd = prefetch;
     h->graph_dirty = true;
     return EWF_OK;
 }
 
-extern "C" int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *ctas)
+extern "C" int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *prefetch, int32_t *ctas)
 {
-    if (!h || !ctas_per_sm || !lag || !ctas) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    if (!h || !ctas_per_sm || !lag || !prefetch || !ctas) return ewf_fail(EWF_ERR_ARG, "NULL argument");
     if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
     *ctas_per_sm = h->sw_per_sm;
     *lag = h->sw_lag;
+    *prefetch = h->sw_pfd;
     *ctas = h->sw_ctas;
     return EWF_OK;
 }

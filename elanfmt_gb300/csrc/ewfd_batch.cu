@@ -429,6 +429,9 @@ static int build_tables(ewf_batch *b)
         d.c66 = (float)p.c66; d.bx = (float)p.bx; d.by = (float)p.by; d.bz = (float)p.bz;
         d.third = 1.0f / 3.0f;
         d.fdiv = q.fdiv ? 1 : 0;
+        d.bc1 = p.free_surface == EWF_FS_BC1 ? 1 : 0;
+        d.smu_on = p.surface_mu > 0.0 ? 1 : 0;
+        d.smu = (float)p.surface_mu;
         bp.tiles_x = (p.nx + TX - 1) / TX;
         bp.tiles_y = (p.ny + TY - 1) / TY;
         bp.chunks = (p.nz + q.kchunk - 1) / q.kchunk;

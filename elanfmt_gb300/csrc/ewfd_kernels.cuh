@@ -53,6 +53,9 @@ struct StepArgs {
     T third;            // (T)1/(T)3 of BC1
     int fdiv;           // 1: div_spacing may take the reciprocal path for dx, dy, dz (verified)
     T vdamp;            // linear velocity damping (16 km scheme), 0 = off
+    int bc1;            // 1: BC1 after the stress update (stress_store, inject_entry); 0: none
+    int smu_on;         // isotropic 1-D PML scheme: shear modulus smu instead of c66 on plane k = 1
+    T smu;
 };
 
 struct SrcEntry {
@@ -226,7 +229,8 @@ __device__ __forceinline__ void stress_math(const StepArgs<T> &a, const StressIn
         o[0] = cd.wavx * (q.s[0] + dt * (c11 * Vxx + c12 * Vyy + c12 * Vzz));
         o[1] = cd.wavy * (q.s[1] + dt * (c12 * Vxx + c11 * Vyy + c12 * Vzz));
         o[2] = T(0.5) * (q.w + wz_k) * (q.s[2] + dt * (c12 * Vxx + c12 * Vyy + c11 * Vzz));
-        const T c66dt = a.c66 * dt;
+        // the diff_BC2_OK3 scheme's shear modulus on plane 1 (its FastWaveED_GPU3D_v1.cu:309-314)
+        const T c66dt = ((a.smu_on && k == 1) ? a.smu : a.c66) * dt;
         // OK4:323, 326, 329 (no guards: zero-padded neighbours at the low edges)
         o[3] = wz_k * cd.wyj * cd.wxi * (q.s[3] + c66dt * ((q.vy - q.vy_im) * rdx + (q.vx - q.vx_jm) * rdy));
         o[4] = cd.wyj * wz_k * cd.wxi * (q.s[4] + c66dt * ((vz_k - q.vz_im) * rdx + (q.vx - vx_m) * rdz));
@@ -268,19 +272,19 @@ __device__ __forceinline__ void stress_math(const StepArgs<T> &a, const StressIn
     }
 }
 
-// Stores the new stresses of cell c (plane k; sys: state plane pitch), with BC1: szz = 0 on plane
-// 0 and, from the freshly updated plane 2, sxz / syz on plane 1 (OK4:279-282).
+// Stores the new stresses of cell c (plane k; sys: state plane pitch), with BC1 (when a.bc1):
+// szz = 0 on plane 0 and, from the freshly updated plane 2, sxz / syz on plane 1 (OK4:279-282).
 template <typename T>
 __device__ __forceinline__ void stress_store(const StepArgs<T> &a, long long c, long long sys, int k, int i, int j,
                                              bool row_bc, const T (&o)[6], bool w_xy, bool w_xz, bool w_yz)
 {
     a.f[3][c] = o[0];
     a.f[4][c] = o[1];
-    a.f[5][c] = (k == 0 && row_bc) ? T(0) : o[2];
+    a.f[5][c] = (k == 0 && row_bc && a.bc1) ? T(0) : o[2];
     if (w_xy) a.f[6][c] = o[3];
     if (w_xz) a.f[7][c] = o[4];
     if (w_yz) a.f[8][c] = o[5];
-    if (k == 2) {
+    if (k == 2 && a.bc1) {
         if (i > 0 && row_bc) a.f[7][c - sys] = a.third * o[4];
         if (j > 0) a.f[8][c - sys] = a.third * o[5];
     }
@@ -347,9 +351,9 @@ __device__ __forceinline__ void inject_entry(const StepArgs<T> &a, const SrcEntr
     const long long c = (long long)q.i * a.R + (long long)q.j * a.sxs + (long long)q.k * a.sys;
     T *f = a.f[q.comp];
     if (order == 0) {
-        const bool row_bc = q.j < a.bc1_rows;
+        const bool row_bc = a.bc1 && q.j < a.bc1_rows;
         const bool xz_bc = (q.comp == 7) && q.i > 0 && q.i < a.nx && row_bc;
-        const bool yz_bc = (q.comp == 8) && q.j > 0 && q.j < a.ny && q.i < a.nx;
+        const bool yz_bc = a.bc1 && (q.comp == 8) && q.j > 0 && q.j < a.ny && q.i < a.nx;
         if ((q.comp == 5 && q.k == 0 && row_bc) || ((xz_bc || yz_bc) && q.k == 1)) return;
         f[c] = f[c] + (T)q.coef * s;
         if ((xz_bc || yz_bc) && q.k == 2) f[c - a.sys] = a.third * f[c];
@@ -386,10 +390,9 @@ struct VelIn {
     T cp[KAHAN ? 3 : 1];
 };
 
-// State part of a cell's velocity inputs (c: state index, x stride R): the stresses around the
-// cell and the old velocities.
+// The stresses around a cell that its velocity update reads (c: state index, x stride R).
 template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, int COH = 0>
-__device__ __forceinline__ void vel_load_state(const StepArgs<T> &a, long long c, VelIn<T, MODEL, DAMP, KAHAN> &q)
+__device__ __forceinline__ void vel_load_sigma(const StepArgs<T> &a, long long c, VelIn<T, MODEL, DAMP, KAHAN> &q)
 {
     const int R = RC ? RC : a.R;
     const int sx = (RC == 1) ? a.sx : a.sxs;
@@ -406,6 +409,13 @@ __device__ __forceinline__ void vel_load_state(const StepArgs<T> &a, long long c
     q.sxz_ip = lds<COH>(a.f[7] + c + R);
     q.syz_p = lds<COH>(a.f[8] + c + sy);
     q.syz_jp = lds<COH>(a.f[8] + c + sx);
+}
+
+// State part of a cell's velocity inputs: the stresses around the cell and the old velocities.
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, int COH = 0>
+__device__ __forceinline__ void vel_load_state(const StepArgs<T> &a, long long c, VelIn<T, MODEL, DAMP, KAHAN> &q)
+{
+    vel_load_sigma<T, MODEL, DAMP, KAHAN, RC, COH>(a, c, q);
 #pragma unroll
     for (int f = 0; f < 3; ++f) q.v[f] = a.f[f][c];
 }

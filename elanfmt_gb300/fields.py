@@ -14,6 +14,7 @@ PREC_F32, PREC_F32_KAHAN, PREC_F64 = 0, 1, 2
 STEP_SPLIT, STEP_FUSED, STEP_WAVE, STEP_SWEEP = 0, 1, 2, 3   # ewf_params.fused: the step form
 DAMP_PML1D, DAMP_W3D, DAMP_SEPARABLE, DAMP_PERCOMP = 0, 1, 2, 3
 SRC_BEFORE_BC1, SRC_AFTER_BC1 = 0, 1
+FS_BC1, FS_NONE = 0, 1   # ewf_params.free_surface
 
 # state fields
 F_VX, F_VY, F_VZ, F_SXX, F_SYY, F_SZZ, F_SXY, F_SXZ, F_SYZ = range(9)

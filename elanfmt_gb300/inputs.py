@@ -314,6 +314,55 @@ def ricker_stf(nt: int, dt: float, f0: float, t0: float | None = None, scale: fl
     return scale * f0 * np.diff(R)
 
 
+def matlab_colon(a: float, step: float, b: float) -> np.ndarray:
+    """a:step:b as MATLAB's colon forms it -- n = floor((b - a)/step) + 1 elements (a relative
+    tolerance of a few ulps admits the end point), element k = a + k*step.  MATLAB may round
+    the second half of a long range from the far end instead; that differs in the last bit at
+    most, below what a float32 Src.dat keeps."""
+    n = int(math.floor((b - a) / step * (1.0 + 4 * np.finfo(float).eps))) + 1
+    return a + step * np.arange(max(n, 0), dtype=np.float64)
+
+
+def stf_isotropic_driver(nt: int, nx: int, lx: float, lam: float = 350.0, amp: float = 3.3 * 2e9,
+                         shift: int = 199) -> np.ndarray:
+    """The Src the isotropic MATLAB driver writes (FINAL.m:372-413, the last SourceGauss it builds):
+    a Gaussian in the model's own x grid, init = amp exp(-(x / lam)^2) with x = -Lx/2 : dx : Lx/2,
+    dx = Lx / (nx - 1) (FINAL.m:151, 373-381), shifted so that Src(1 : nx-shift) =
+    init(shift+1 : end) (:395) and zero after.  Peak 6.6e9 with the driver's constants.  Needs no
+    srctimefun.txt: the driver loads that file only for SourceSharp, which Src does not use.
+    Returns FP64 samples (the driver writes them as float32)."""
+    dx = lx / (nx - 1)
+    x = matlab_colon(-lx / 2, dx, lx / 2)[:nx]
+    init = amp * np.exp(-(x / lam) ** 2)
+    n = nx - shift
+    if n < 1:
+        raise ValueError(f"nx = {nx}: the driver's shift of {shift} samples leaves no source")
+    if n > nt:
+        raise ValueError(f"Src(1:{n}) does not fit in nt = {nt} samples")
+    src = np.zeros(nt)
+    src[:n] = init[shift:shift + n]
+    return src
+
+
+def stf_orthorhombic_driver(nt: int, dx: float, dur: int = 400, lam: float = 1000.0, peak: float = 2.5e-3) -> np.ndarray:
+    """The Src the orthorhombic MATLAB driver writes (ANIS.m:522-533): on the grid
+    x = -20 dur : dx : 20 dur, init = peak exp(-(x / lam / 2)^2); SourceGauss(1 : 2 dur - 3) =
+    -1e9 diff(diff(init)) (a negative second derivative of a Gaussian, Ricker-like), then scaled
+    to a maximum of `peak` (2.5e-3).  The assignment needs exactly 2 dur - 1 grid points, as in the
+    driver (dx = 15360 / 767 there); other spacings raise, as MATLAB's dimension check does.
+    srctimefunL.txt, which the driver also loads, is only plotted."""
+    x = matlab_colon(-dur * 20.0, dx, dur * 20.0)
+    init = peak * np.exp(-(x / lam / 2) ** 2)
+    g = -1e9 * np.diff(np.diff(init))
+    if len(g) != 2 * dur - 3:
+        raise ValueError(f"dx = {dx}: {len(x)} grid points give {len(g)} samples, the driver assigns {2 * dur - 3}")
+    if 2 * dur - 3 > nt:
+        raise ValueError(f"Src(1:{2 * dur - 3}) does not fit in nt = {nt} samples")
+    src = np.zeros(nt)
+    src[:len(g)] = g
+    return src / src.max() * peak
+
+
 # ---------------------------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------------------------
@@ -340,6 +389,8 @@ class Model:
     by: float = 0.0
     bz: float = 0.0
     vdamp: float = 0.0    # linear velocity damping of the 16 km scheme (0 = off)
+    free_surface: int = F.FS_BC1   # F.FS_NONE: no BC1 (the diff_BC schemes)
+    surface_mu: float = 0.0        # isotropic scheme: shear modulus on plane k = 1 when > 0 (0 = c66 there too)
     c44: float = 0.0      # per-component-weight scheme: shear moduli of yz and xz (c66: xy)
     c55: float = 0.0
     materials: dict = field(default_factory=dict)   # field id -> float32 array

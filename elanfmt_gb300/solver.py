@@ -37,6 +37,7 @@ class Params(C.Structure):
         ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
         ("vdamp", C.c_double),
         ("workdir", C.c_char_p),
+        ("free_surface", C.c_int32), ("reserved", C.c_int32), ("surface_mu", C.c_double),
     ]
 
 
@@ -76,8 +77,9 @@ SIGNATURES = {
     "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_wave_hold": (C.c_int, [C.c_void_p, C.c_int32]),
-    "ewf_set_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
-    "ewf_get_sweep": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ewf_set_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "ewf_get_sweep": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                C.POINTER(C.c_int32)]),
     "ewf_sweep_hold": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_batch_create": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ewf_batch_destroy": (None, [C.c_void_p]),
@@ -97,6 +99,8 @@ SIGNATURES = {
     "ewf_mlp_gemm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_mlp_status": (C.c_int, []),
+    "ewf_sosfilt": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_int64]),
+    "ewf_sosfilt_device": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]),
     "ewf_mlp_test_hold": (C.c_int, [C.c_int32, C.c_int32]),
     "ewf_mlp_transpose": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_mlp_gelu_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
@@ -174,6 +178,8 @@ class Solver:
         p.c66, p.bx, p.by, p.bz = m.c66, m.bx, m.by, m.bz
         p.c44, p.c55 = getattr(m, "c44", 0.0), getattr(m, "c55", 0.0)
         p.vdamp = getattr(m, "vdamp", 0.0)
+        p.free_surface = getattr(m, "free_surface", F.FS_BC1)
+        p.surface_mu = getattr(m, "surface_mu", 0.0)
         if fused is not None:
             p.fused = int(fused)
         if workdir is not None:
@@ -293,15 +299,16 @@ class Solver:
         _check(self._lib.ewf_get_wave(self._h, C.byref(lag)), "ewf_get_wave")
         return lag.value
 
-    def set_sweep(self, ctas_per_sm: int, lag: int) -> None:
-        """Sweep step: CTAs per multiprocessor and velocity lag (results do not depend on them)."""
-        _check(self._lib.ewf_set_sweep(self._h, int(ctas_per_sm), int(lag)), "ewf_set_sweep")
+    def set_sweep(self, ctas_per_sm: int, lag: int, prefetch: int = 4) -> None:
+        """Sweep step: CTAs per multiprocessor, velocity lag and L2 prefetch distance in planes
+        (results do not depend on them)."""
+        _check(self._lib.ewf_set_sweep(self._h, int(ctas_per_sm), int(lag), int(prefetch)), "ewf_set_sweep")
 
-    def sweep_layout(self) -> tuple[int, int, int]:
-        """Sweep step: (CTAs per multiprocessor, lag, CTAs of the layout last built)."""
-        m, lag, n = C.c_int32(), C.c_int32(), C.c_int32()
-        _check(self._lib.ewf_get_sweep(self._h, C.byref(m), C.byref(lag), C.byref(n)), "ewf_get_sweep")
-        return m.value, lag.value, n.value
+    def sweep_layout(self) -> tuple[int, int, int, int]:
+        """Sweep step: (CTAs per multiprocessor, lag, prefetch distance, CTAs of the layout last built)."""
+        m, lag, pf, n = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        _check(self._lib.ewf_get_sweep(self._h, C.byref(m), C.byref(lag), C.byref(pf), C.byref(n)), "ewf_get_sweep")
+        return m.value, lag.value, pf.value, n.value
 
     def sweep_hold(self, cta: int) -> None:
         _check(self._lib.ewf_sweep_hold(self._h, int(cta)), "ewf_sweep_hold")

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define EWF_ABI_VERSION 3
+#define EWF_ABI_VERSION 4
 
 typedef enum ewf_status {
     EWF_OK = 0,
@@ -81,6 +81,14 @@ typedef enum ewf_step_form {
                          * precision; grids up to about 2 x 152 x 736 columns nx*ny in FP32) */
 } ewf_step_form;
 
+typedef enum ewf_free_surface {
+    EWF_FS_BC1 = 0,  /* BC1 after the stress update: szz = 0 on plane 0, sxz/syz on plane 1 = plane 2 / 3
+                      * (OK4:271-283, ANISO:270-285; every shipped scheme but the two below) */
+    EWF_FS_NONE = 1  /* no BC1: the stress planes are left as updated -- the "diff_BC" schemes, whose
+                      * BC1 launch is commented out (src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_diff_BC_OK2/
+                      * FastWaveED_GPU3D_v1.cu:453, ..._diff_BC2_OK3/FastWaveED_GPU3D_v1.cu:476) */
+} ewf_free_surface;
+
 typedef enum ewf_src_order {
     EWF_SRC_BEFORE_BC1 = 0, /* OK4: injection inside the stress kernel, BC1 after (OK4:336-342, 490) */
     EWF_SRC_AFTER_BC1 = 1   /* ANISO: BC1, then the source kernel (ANISO:533-535) */
@@ -131,6 +139,12 @@ typedef struct ewf_params {
                             * scheme, FastWaveED_GPU3D_v1_16kmst.cu:337-349, vdamp = 2.2 * 4.6729e-04
                             * in float); 0 = off.  Models 1 and 2, FP32 / FP64, not the one-pass step. */
     const char *workdir;   /* legacy *.dat inputs and *.res outputs (NULL = ".") */
+    int32_t free_surface;  /* ewf_free_surface: 0 (default) BC1, 1 none; not the one-pass step */
+    int32_t reserved;      /* 0 */
+    double surface_mu;     /* isotropic scheme with 1-D PML: > 0 replaces the shear modulus c66 on the plane
+                            * k = 1 (the diff_BC2_OK3 scheme's c44u = 1e-5 there,
+                            * ..._diff_BC2_OK3/FastWaveED_GPU3D_v1.cu:309-314); 0 = off; not the one-pass
+                            * step.  The other schemes carry such a layer in their edge shear-modulus fields. */
 } ewf_params;
 
 typedef struct ewf_handle ewf_handle;
@@ -215,12 +229,13 @@ int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct);
  * usable after ewf_reset).  -1 restores normal operation. */
 int ewf_wave_hold(ewf_handle *h, int32_t item);
 
-/* Sweep step (fused = EWF_STEP_SWEEP): CTAs per multiprocessor (1..8; all CTAs must fit at once)
- * and the lag of the velocity plane behind the stress plane (2..16), both set by ewf_autotune;
- * results do not depend on them.  ewf_get_sweep also returns the CTAs of the layout last built
- * (0 before the first run).  EWF_ERR_STATE for the other step forms. */
-int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag);
-int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *ctas);
+/* Sweep step (fused = EWF_STEP_SWEEP): CTAs per multiprocessor (1..8; all CTAs must fit at once),
+ * the lag of the velocity plane behind the stress plane (3..16) and how many planes ahead the
+ * control warp prefetches the inputs into L2 (0..32, 0 = off), all set by ewf_autotune; results do
+ * not depend on them.  ewf_get_sweep also returns the CTAs of the layout last built (0 before the
+ * first run).  EWF_ERR_STATE for the other step forms. */
+int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag, int32_t prefetch);
+int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *prefetch, int32_t *ctas);
 /* Diagnostic for tests of the failure path: CTA `cta` of the sweep step never publishes its
  * progress, so its neighbours give up after their bounded wait and ewf_run returns EWF_ERR_CUDA
  * (the state of that run is invalid; the handle stays usable after ewf_reset).  -1 restores
@@ -267,6 +282,18 @@ int ewf_snapshot_wait(ewf_handle *h);
 #define EWF_NOALLOC_SCRATCH_BYTES (16u << 20)
 int ewf_pack_field_noalloc(void *dst, int32_t dst_dtype_bytes, int32_t sx, int64_t sy, const void *host,
                            int32_t host_dtype_bytes, int32_t ex, int32_t ey, int32_t ez, void *stream);
+
+/* Seismogram post-processing: a cascade of second-order IIR sections applied in place to `ntr`
+ * traces of `n` samples each (trace-major), FP64 -- the isotropic MATLAB driver's 4th-order
+ * Butterworth band-pass, `sos = zp2sos(butter(4, [flo fhi], 'bandpass')); y = sosfilt(sos, x)`
+ * (src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_OK4_final/vizme_FastBiotED_GPU3D_OK_2024_final.m
+ * :551-558, 579-582, 604-607).  sos: nsec rows of (b0 b1 b2 a0 a1 a2) as MATLAB and scipy lay
+ * them out; each section is the direct form II transposed recursion from zero state.
+ * ewf_sosfilt works on host arrays; ewf_sosfilt_device on device arrays (one thread per trace,
+ * on `stream`), with the same bits. */
+#define EWF_SOS_MAX_SECTIONS 16
+int ewf_sosfilt(const double *sos, int32_t nsec, double *x, int64_t ntr, int64_t n);
+int ewf_sosfilt_device(const double *sos, int32_t nsec, double *x, int64_t ntr, int64_t n, void *stream);
 
 /* Checkpoint / resume: state fields, compensation, traces and step counter. */
 int ewf_checkpoint(ewf_handle *h, const char *path);

@@ -5,8 +5,9 @@
 * ``_ref/*.cubin``     -- the reference solvers' device code compiled from the reference sources
   where they lie (only where the reference tree is present; the cubins then travel with the
   repository copy).  The isotropic (OK4), orthorhombic (ANISO), 9 km (isotropic with edge shear
-  moduli), 16 km (the 9 km scheme with linear velocity damping) and DC_Earthquake (isotropic
-  with per-component weights) solvers, each with the
+  moduli), 16 km (the 9 km scheme with linear velocity damping), DC_Earthquake (isotropic
+  with per-component weights), the two BC1-free isotropic variants (diff_BC2_OK3, diff_BC_OK2)
+  and the FULL scheme (3-D weights, scalar moduli), each with the
   reference's own flags (``-O3``, FMA contraction on: "stock") and with ``--fmad=false``
   ("exact", every operation rounded on its own, which the oracle matches bit for bit).
 
@@ -25,13 +26,20 @@ REF_OUT = os.path.join(HERE, "_ref")
 ORACLE_LIB = os.path.join(HERE, "libewf_oracle.so")
 REFK_LIB = os.path.join(HERE, "librefkernels.so")
 
-REFERENCE_ROOT = "/root/reference"
+# where the reference sources lie (only this build step reads them); override with EWF_REFERENCE_ROOT
+REFERENCE_ROOT = os.environ.get("EWF_REFERENCE_ROOT", "/root/reference")
 REF_SOURCES = {
     "ok4": "src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_OK4_final/FastWaveED_GPU3D_v1.cu",
     "aniso": "src/FastWaveED_GPU3D_v1_9km_station_ANISO/FastWaveED_GPU3D_v1_9kmst_ANISO.cu",
     "iso9km": "src/FastWaveED_GPU3D_v1_9km_station/FastWaveED_GPU3D_v1_9kmst.cu",
     "iso16km": "src/FastWaveED_GPU3D_v1_16km_station/FastWaveED_GPU3D_v1_16kmst.cu",
     "dcq": "src/FastWaveED_GPU3D_v1_DC_Earthquake/FastWaveED_GPU3D_v1.cu",
+    # isotropic without BC1, shear modulus 1e-5 on plane 1 (the diff_BC2 scheme)
+    "ok3": "src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_diff_BC2_OK3/FastWaveED_GPU3D_v1.cu",
+    # the 3-D-weight isotropic form with scalar moduli, without BC1 (the diff_BC scheme)
+    "ok2": "src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_diff_BC_OK2/FastWaveED_GPU3D_v1.cu",
+    # the same form with BC1 and a separate source kernel
+    "full": "src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL/FastBiot_GPU3D_v1.cu",
 }
 # The grid defines only size the host-side constants of the reference; every kernel takes
 # nx, ny, nz as arguments, so one build serves every grid.

@@ -10,7 +10,8 @@
  *   isotropic stress + 1-D PML      src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_OK4_final/FastWaveED_GPU3D_v1.cu:285-331
  *   moment-tensor injection         same file :336-342 (before BC1) and
  *                                   src/FastWaveED_GPU3D_v1_9km_station_ANISO/FastWaveED_GPU3D_v1_9kmst_ANISO.cu:228-252 (after BC1)
- *   free surface BC1                OK4 :271-283, ANISO :270-285
+ *   free surface BC1                OK4 :271-283, ANISO :270-285 (left out by the two diff_BC schemes)
+ *   plane-1 shear modulus           src/FastWaveED_GPU3D_v1_DC_Earthquake_FULL_diff_BC2_OK3/FastWaveED_GPU3D_v1.cu:309-323
  *   isotropic velocity update       OK4 :346-378
  *   orthorhombic stress update      ANISO :287-356
  *   orthorhombic velocity update    ANISO :358-389
@@ -44,7 +45,10 @@ typedef struct orc_grid {
     double vdamp;      /* linear velocity damping (16 km scheme), 0 = off */
     double c44, c55;   /* per-component-weight scheme: shear moduli of yz and xz (c66: xy) */
     int32_t damping;   /* 3 = per-component weights (w[0..5]: Vx/sxx, Vy/syy, Vz/szz, sxy, sxz, syz) */
-    int32_t pad;
+    int32_t no_bc1;    /* 1 = no BC1 (the diff_BC schemes: ..._diff_BC_OK2/FastWaveED_GPU3D_v1.cu:453,
+                        * ..._diff_BC2_OK3/FastWaveED_GPU3D_v1.cu:476 comment its launch out) */
+    double smu;        /* > 0: the isotropic scheme's shear modulus on plane k = 1
+                        * (..._diff_BC2_OK3/FastWaveED_GPU3D_v1.cu:309-314, c44u = 1e-5 there) */
 } orc_grid;
 
 #define OT float
@@ -59,7 +63,7 @@ typedef struct orc_grid {
 #undef OT
 #undef OSUF
 
-int orc_abi_version(void) { return 3; }
+int orc_abi_version(void) { return 4; }
 
 int orc_num_threads(void)
 {

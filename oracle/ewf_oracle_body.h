@@ -30,7 +30,7 @@ static void OFN(stress_iso)(const orc_grid *g, OT *const *f, const OT *const *m,
 {
     const long nx = g->nx, ny = g->ny, nz = g->nz;
     const OT dt = (OT)g->dt, rdx = (OT)1.0 / (OT)g->dx, rdy = (OT)1.0 / (OT)g->dy, rdz = (OT)1.0 / (OT)g->dz;
-    const OT c66 = (OT)g->c66;
+    const OT c66s = (OT)g->c66;
     const OT *Vx = f[0], *Vy = f[1], *Vz = f[2];
     OT *sxx = f[3], *syy = f[4], *szz = f[5], *sxy = f[6], *sxz = f[7], *syz = f[8];
     const OT *c11 = m[0], *c12 = m[1];
@@ -41,6 +41,8 @@ static void OFN(stress_iso)(const orc_grid *g, OT *const *f, const OT *const *m,
         for (long j = 0; j < ny; j++) {
             for (long i = 0; i < nx; i++) {
                 const long c = i + nx * (j + ny * k);
+                /* the diff_BC2_OK3 scheme's c44u: its own value on plane 1, c66 elsewhere */
+                const OT c66 = (g->smu > 0.0 && k == 1) ? (OT)g->smu : c66s;
                 const OT Vxx = (Vx[(i + 1) + (nx + 1) * (j + ny * k)] - Vx[i + (nx + 1) * (j + ny * k)]) * rdx;
                 const OT Vyy = (Vy[i + nx * ((j + 1) + (ny + 1) * k)] - Vy[i + nx * (j + (ny + 1) * k)]) * rdy;
                 const OT Vzz = (Vz[i + nx * (j + ny * (k + 1))] - Vz[i + nx * (j + ny * k)]) * rdz;
@@ -431,7 +433,7 @@ int OFN(orc_run)(const orc_grid *g, OT *const *f, OT *const *comp, const OT *con
         else if (g->model == 2) OFN(stress_isohet)(g, f, m, W);
         else                    OFN(stress_ortho)(g, f, m, W);
         if (g->src_order == 0) OFN(inject)(g, f, nsrc, src, coef, stf, it);
-        OFN(bc1)(g, f);
+        if (!g->no_bc1) OFN(bc1)(g, f);
         if (g->src_order != 0) OFN(inject)(g, f, nsrc, src, coef, stf, it);
         OFN(velocity)(g, f, m, w, W, comp);
         OFN(record)(g, f, nrec, rec, traces, trace_len, it);

@@ -24,7 +24,7 @@ class Grid(C.Structure):
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("dt", C.c_double),
                 ("c66", C.c_double), ("bx", C.c_double), ("by", C.c_double), ("bz", C.c_double),
                 ("vdamp", C.c_double), ("c44", C.c_double), ("c55", C.c_double), ("damping", C.c_int32),
-                ("pad", C.c_int32)]
+                ("no_bc1", C.c_int32), ("smu", C.c_double)]
 
 
 _lib = None
@@ -89,7 +89,8 @@ class Runner:
         self.state = state
         self.grid = Grid(m.nx, m.ny, m.nz, m.model, m.src_order, bc1_rows(m), m.dx, m.dy, m.dz, m.dt, m.c66, m.bx,
                          m.by, m.bz, getattr(m, "vdamp", 0.0), getattr(m, "c44", 0.0), getattr(m, "c55", 0.0),
-                         m.damping, 0)
+                         m.damping, int(getattr(m, "free_surface", F.FS_BC1) == F.FS_NONE),
+                         float(getattr(m, "surface_mu", 0.0)))
         cv = lambda a: np.ascontiguousarray(a, dtype=dtype)  # noqa: E731
         if m.model == F.MODEL_ISO:
             self.mats = [cv(m.materials[F.M_C11]), cv(m.materials[F.M_C12])]

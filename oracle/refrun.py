@@ -9,6 +9,8 @@ FastWaveED_GPU3D_v1_9kmst_ANISO.cu:391-608): allocation, the launch geometry
   orthorhombic:  compute_StressOrtho, BC1, source, update_VelocityFromStress (ANISO:519-555)
   9 km / 16 km:  compute_StressPrf, BC1, source, update_Qxft            (9kmst.cu:463-477)
   DC_Earthquake: compute_StressPrf, BC1, source, update_Qxft            (FastWaveED_GPU3D_v1.cu:473-483)
+  diff_BC2_OK3, diff_BC_OK2: compute_StressPrf (source inside), update_Qxft -- no BC1 (:473-483, :450-460)
+  FULL:          compute_StressPrf, BC1, source, update_Qxft            (FastBiot_GPU3D_v1.cu:441-451)
 with our receivers gathered from V after each step (a read-only gather; the reference's own
 hard-coded `record` cells are left as they are).
 
@@ -60,16 +62,23 @@ def _ck(st: int, what: str) -> None:
         raise RuntimeError(f"{what}: {lib().refk_error().decode(errors='replace')}")
 
 
-def cubin(model: int, variant: str, vdamp: float = 0.0, damping: int = -1) -> str:
-    if model == F.MODEL_ISO and damping == F.DAMP_PERCOMP:
+# reference schemes selected by Model.meta["scheme"] rather than by model and damping alone
+SCHEMES = ("ok3", "ok2", "full")
+
+
+def cubin(model: int, variant: str, vdamp: float = 0.0, damping: int = -1, scheme: str | None = None) -> str:
+    if scheme in SCHEMES:
+        name = scheme
+    elif model == F.MODEL_ISO and damping == F.DAMP_PERCOMP:
         name = "dcq"
     else:
         name = {F.MODEL_ISO: "ok4", F.MODEL_ORTHO: "aniso"}.get(model, "iso16km" if vdamp else "iso9km")
     return os.path.join(HERE, "_ref", f"{name}_{variant}.cubin")
 
 
-def available(model: int = F.MODEL_ISO, variant: str = "exact", vdamp: float = 0.0, damping: int = -1) -> bool:
-    return os.path.exists(cubin(model, variant, vdamp, damping))
+def available(model: int = F.MODEL_ISO, variant: str = "exact", vdamp: float = 0.0, damping: int = -1,
+              scheme: str | None = None) -> bool:
+    return os.path.exists(cubin(model, variant, vdamp, damping, scheme))
 
 
 def trace_errors(ours: np.ndarray, ref: np.ndarray) -> dict:
@@ -122,8 +131,9 @@ class RefRunner:
         torch.zeros(1, device=self.dev)
         _ck(lib().refk_init(device), "refk_init")
         mod = C.c_void_p()
-        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant, getattr(m, "vdamp", 0.0), m.damping)), C.byref(mod)),
-            "refk_load")
+        self.scheme = (getattr(m, "meta", None) or {}).get("scheme")
+        _ck(lib().refk_load(os.fsencode(cubin(m.model, variant, getattr(m, "vdamp", 0.0), m.damping, self.scheme)),
+                            C.byref(mod)), "refk_load")
         self.mod = mod
         nx, ny, nz = m.nx, m.ny, m.nz
         self.pad = (nx + 2) * (ny + 2) + 64
@@ -198,7 +208,10 @@ class RefRunner:
         f = self.f
         nx, ny, nz = m.nx, m.ny, m.nz
         d = self.dummy
-        if m.model == F.MODEL_ISO and m.damping == F.DAMP_PERCOMP:
+        self.bc1 = True
+        if self.scheme in SCHEMES:
+            self._setup_diff_bc()
+        elif m.model == F.MODEL_ISO and m.damping == F.DAMP_PERCOMP:
             if m.src_order != F.SRC_AFTER_BC1:
                 raise ValueError("DC_Earthquake reference = after-BC1 injection")
             xs, ys, zs = self._check_sources(1)
@@ -347,6 +360,103 @@ class RefRunner:
             + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", 0), ("i", 0), ("i", 0), ("i", 2)] + [("f", m.dt)])
         self.it_pos_bc1 = 16 + 9 + 3
 
+    def _setup_diff_bc(self):
+        """The isotropic variants of the DC_Earthquake FULL family: their sources are built in
+        (sigma_yz += 0.8 Src at (xs+2, ys+2, zs+1), sigma_xz += 1.0 Src at (xs+3, ys+3, zs+1))."""
+        m, P, f, d = self.m, self._p, self.f, self.dummy
+        nx, ny, nz = m.nx, m.ny, m.nz
+        xs, ys, zs = self._check_sources(0)
+        coef = tuple(float(np.float32(v)) for v in self._mt_tuple())
+        if coef != (0.0, 0.0, 0.0, 0.0, 1.0, float(np.float32(0.8))):
+            raise ValueError("the diff_BC / FULL references hard-code their source: xz 1.0, yz 0.8")
+        c11 = self._upload(m.materials[F.M_C11])
+        c12 = self._upload(m.materials[F.M_C12])
+        it_src = []
+        if self.scheme == "ok3":
+            # OK4's kernels without the tensor arguments; no BC1 launch (FastWaveED_GPU3D_v1.cu:473-483)
+            if m.model != F.MODEL_ISO or m.damping != F.DAMP_PML1D:
+                raise ValueError("the diff_BC2_OK3 reference: isotropic model, 1-D PML")
+            wx, wy, wz = (self._upload(m.damping_arrays[k]) for k in (F.D_WX, F.D_WY, F.D_WZ))
+            R = self.rec_dummy
+            self.k_stress = self._fn("_Z17compute_StressPrf")
+            self.a_stress = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 3
+                + [("p", P(c11)), ("p", P(c12)), ("p", P(wx)), ("p", P(wy)), ("p", P(wz))]
+                + [("p", P(r)) for r in R] + [("p", P(self.src))]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 8 + [("f", m.c66)]
+                + [("f", 0.0)] * 4 + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)])
+            self.it_pos_stress = 23 + 17 + 3
+            self.k_vel = self._fn("_Z11update_Qxft")
+            self.a_vel = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 7
+                + [("p", P(wx)), ("p", P(wy)), ("p", P(wz))] + [("p", P(r)) for r in R]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt), ("f", 0.0), ("f", 0.0), ("f", 0.0),
+                   ("f", m.bx), ("f", m.by), ("f", m.bz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5), ("i", 0)])
+            self.it_pos_vel = 24 + 16 + 3 + 1
+            self.k_src = None
+            self.bc1 = False
+            return
+        # ok2 / full: c11/c12 cell fields, one 3-D weight field, scalar shear moduli and buoyancy
+        # (the product's 9 km scheme with constant edge-modulus and buoyancy fields)
+        if m.model != F.MODEL_ISO_HET or F.D_W3D not in m.damping_arrays:
+            raise ValueError("the diff_BC_OK2 / FULL references: the 9 km scheme's form with 3-D weights")
+        W = self._upload(m.damping_arrays[F.D_W3D])
+        c44, c55, c66 = (float(np.asarray(m.materials[k]).flat[-1]) for k in (F.M_C44YZ, F.M_C55XZ, F.M_C66XY))
+        bx, by, bz = (float(np.asarray(m.materials[k]).flat[-1]) for k in (F.M_BX, F.M_BY, F.M_BZ))
+        R = self.rec_dummy
+        if self.scheme == "ok2":
+            # compute_StressPrf(Prf, 6 stresses, Vx, Vy, Vz, Qxft..Qzft, c11u_het, c12u_het, weights,
+            # Rec x4, Src, dx, dy, dz, dt, c11u..c66u, alpha1-3, M1, nx, ny, nz, it, xsrc, ysrc, zsrc, ds)
+            self.k_stress = self._fn("_Z17compute_StressPrf")
+            self.a_stress = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 3
+                + [("p", P(c11)), ("p", P(c12)), ("p", P(W))] + [("p", P(r)) for r in R] + [("p", P(self.src))]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 6
+                + [("f", c44), ("f", c55), ("f", c66)] + [("f", 0.0)] * 4
+                + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)])
+            self.it_pos_stress = 21 + 17 + 3
+            # update_Qxft(Prf, 6 stresses, Vx, Vy, Vz, Qxft..Qzold (6), vrhox11het, weights, Rec x4,
+            # dx, dy, dz, dt, eta_k1-3, vrho_x/y/z_11, 6 unused, nx, ny, nz, chi, it)
+            self.k_vel = self._fn("_Z11update_Qxft")
+            self.a_vel = _Args(
+                [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 7
+                + [("p", P(W))] + [("p", P(r)) for r in R]
+                + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt), ("f", 0.0), ("f", 0.0), ("f", 0.0),
+                   ("f", bx), ("f", by), ("f", bz)] + [("f", 0.0)] * 6
+                + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5), ("i", 0)])
+            self.it_pos_vel = 22 + 16 + 3 + 1
+            self.k_src = None
+            self.bc1 = False
+            return
+        # full: compute_StressPrf(Prf, 6 stresses, Vx, Vy, Vz, Qxft..Qzft, c11u_het, c12u_het, weights,
+        # dx, dy, dz, dt, c11u..c66u, alpha1-3, M1, nx, ny, nz) (FastBiot_GPU3D_v1.cu:279), then BC1,
+        # the source kernel and update_Qxft (:441-451)
+        if m.src_order != F.SRC_AFTER_BC1:
+            raise ValueError("the FULL reference injects after BC1")
+        self.k_stress = self._fn("_Z17compute_StressPrf")
+        self.a_stress = _Args(
+            [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 3
+            + [("p", P(c11)), ("p", P(c12)), ("p", P(W))]
+            + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt)] + [("f", 0.0)] * 6
+            + [("f", c44), ("f", c55), ("f", c66)] + [("f", 0.0)] * 4 + [("i", nx), ("i", ny), ("i", nz)])
+        self.it_pos_stress = None
+        self.k_src = self._fn("_Z6source")
+        self.a_src = _Args(
+            [("p", P(d))] * 4 + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1)] + [("p", P(d))] * 2
+            + [("p", P(self.src))] + [("f", m.dx), ("f", m.dy), ("f", m.dz)] + [("f", 0.0)] * 6
+            + [("i", nx), ("i", ny), ("i", nz), ("i", 0), ("i", xs), ("i", ys), ("i", zs), ("i", 2)]
+            + [("f", m.dt)])
+        self.it_pos_src = 15 + 9 + 3
+        self.k_vel = self._fn("_Z11update_Qxft")
+        self.a_vel = _Args(
+            [("p", P(d))] + [("p", P(f[q])) for q in (3, 4, 5, 6, 7, 8, 0, 1, 2)] + [("p", P(d))] * 7
+            + [("p", P(W))]
+            + [("f", m.dx), ("f", m.dy), ("f", m.dz), ("f", m.dt), ("f", 0.0), ("f", 0.0), ("f", 0.0),
+               ("f", bx), ("f", by), ("f", bz)] + [("f", 0.0)] * 6
+            + [("i", nx), ("i", ny), ("i", nz), ("f", 0.5)])
+        self.it_pos_vel = None
+
     def _mt_tuple(self):
         mt = {int(c): float(v) for (c, *_), v in zip(self.m.sources, self.m.source_coef)}
         return (mt[F.F_SXX], mt[F.F_SYY], mt[F.F_SZZ], mt[F.F_SXY], mt[F.F_SXZ], mt[F.F_SYZ])
@@ -361,8 +471,9 @@ class RefRunner:
             if self.it_pos_stress is not None:
                 self.a_stress.set_int(self.it_pos_stress, it)
             self._launch(self.k_stress, self.a_stress)
-            self.a_bc1.set_int(self.it_pos_bc1, it)
-            self._launch(self.k_bc1, self.a_bc1)
+            if self.bc1:
+                self.a_bc1.set_int(self.it_pos_bc1, it)
+                self._launch(self.k_bc1, self.a_bc1)
             if self.k_src is not None:
                 self.a_src.set_int(self.it_pos_src, it)
                 self._launch(self.k_src, self.a_src)

@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 def test_abi_version_and_strerror(built_lib):
     lib = S.load_library()
-    assert lib.ewf_abi_version() == 3
+    assert lib.ewf_abi_version() == 4
     for code, name in F.STATUS.items():
         assert lib.ewf_strerror(code)
     assert lib.ewf_strerror(-99) == b"unknown status"
@@ -45,8 +45,8 @@ def test_abi_version_and_strerror(built_lib):
 def test_params_struct_layout(built_lib):
     p = S.default_params()
     assert p.model == F.MODEL_ISO and p.precision == F.PREC_F32 and p.check_finite == 1
-    assert p.fused == 0
-    assert C.sizeof(S.Params) == 14 * 4 + 11 * 8 + 8
+    assert p.fused == 0 and p.free_surface == 0 and p.surface_mu == 0.0
+    assert C.sizeof(S.Params) == 14 * 4 + 11 * 8 + 8 + 2 * 4 + 8
 
 
 def _have_gpu():

@@ -49,9 +49,10 @@ CASES = [
 ]
 
 
-FUSED = pytest.mark.parametrize("fused", [F.STEP_FUSED, F.STEP_SPLIT, F.STEP_WAVE], ids=["fused", "split", "wave"])
+FUSED = pytest.mark.parametrize("fused", [F.STEP_FUSED, F.STEP_SPLIT, F.STEP_WAVE, F.STEP_SWEEP],
+                                ids=["fused", "split", "wave", "sweep"])
 # step forms built for every model and damping
-FORMS = pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_WAVE], ids=["split", "wave"])
+FORMS = pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_WAVE, F.STEP_SWEEP], ids=["split", "wave", "sweep"])
 
 
 @pytest.mark.parametrize("name,model,damping,nx,ny,nz", CASES, ids=[c[0] for c in CASES])
@@ -87,6 +88,42 @@ def test_percomp_bitwise_vs_oracle(cuda_device, prec, nx, ny, nz, form):
     m = I.random_small(F.MODEL_ISO, nx, ny, nz, nt=48, seed=nx + 3 * nz, damping=F.DAMP_PERCOMP)
     ref = O.run(m, 48, prec)
     assert_bitwise(product(m, 48, prec, fused=form), ref, "percomp")
+
+
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
+@FORMS
+def test_free_surface_options_bitwise_vs_oracle(cuda_device, prec, form):
+    """No BC1 (the diff_BC schemes), with and without a plane-1 shear modulus on the isotropic
+    scheme, and no BC1 on the orthorhombic and 9 km schemes; sources on planes 0-2."""
+    for model, damping, smu in ((F.MODEL_ISO, None, 1e-5), (F.MODEL_ISO, None, 0.0), (F.MODEL_ORTHO, F.DAMP_W3D, 0.0),
+                                (F.MODEL_ISO_HET, F.DAMP_SEPARABLE, 0.0)):
+        for zs in (0, 1, 6):
+            m = I.random_small(model, 31, 27, 19, nt=36, seed=41 + zs, damping=damping)
+            m.free_surface = F.FS_NONE
+            m.surface_mu = smu
+            m.set_moment_tensor(np.array([0.3, -0.7, 1.1, 0.4, 1.0, 0.8]), 12, 11, zs, 0)
+            ref = O.run(m, 36, prec)
+            assert_bitwise(product(m, 36, prec, fused=form), ref, f"model {model} smu {smu} zs {zs}")
+    m = I.random_small(F.MODEL_ISO, 31, 27, 19, nt=36, seed=47)
+    m.surface_mu = 2e3                 # with BC1 on
+    assert_bitwise(product(m, 36, prec, fused=form), O.run(m, 36, prec), "plane-1 modulus with BC1")
+
+
+def test_free_surface_options_are_checked(cuda_device):
+    m = I.random_small(F.MODEL_ORTHO, 24, 24, 16, nt=4, seed=3, damping=F.DAMP_W3D)
+    m.surface_mu = 1e-5
+    with pytest.raises(EwfError) as e:
+        Solver.from_model(m)
+    assert e.value.status == -8
+    m = I.random_small(F.MODEL_ISO, 24, 24, 16, nt=4, seed=3)
+    m.free_surface = F.FS_NONE
+    with pytest.raises(EwfError) as e:
+        Solver.from_model(m, fused=F.STEP_FUSED)
+    assert e.value.status == -8
+    m.free_surface = 7
+    with pytest.raises(EwfError) as e:
+        Solver.from_model(m)
+    assert e.value.status == -1
 
 
 @pytest.mark.parametrize("model", [F.MODEL_ORTHO, F.MODEL_ISO_HET], ids=["ortho", "isohet"])
@@ -207,12 +244,71 @@ def test_wave_wait_gives_up_and_handle_recovers(cuda_device):
     assert_bitwise(got, ref, "after recovery")
 
 
-def test_workload_shapes_small(cuda_device):
+def sweep_case():
+    """A grid of a few hundred sweep CTAs with point sources on CTA-range borders, on several
+    entries of one cell, and on cells the stress pass never updates (sxy at i = nx and at i = 0,
+    sxz and syz on plane nz): their values are carried over from the previous step."""
+    m = I.random_small(F.MODEL_ORTHO, 100, 72, 40, nt=24, seed=29, damping=F.DAMP_W3D, src_order=F.SRC_BEFORE_BC1)
+    ent, coef = [], []
+    for comp in range(3, 9):
+        for (i, j, k) in ((31, 0, 3), (32, 0, 4), (99, 2, 2), (0, 3, 1), (50, 40, 20), (51, 40, 2), (50, 41, 39)):
+            ent.append((comp, i, j, k))
+            coef.append(0.1 * (comp - 5) + 0.01 * i + 0.001 * k)
+    ent += [(6, 100, 5, 3), (7, 100, 4, 40), (8, 3, 72, 40), (6, 0, 9, 6), (6, 0, 9, 6), (5, 50, 40, 20)]
+    coef += [0.3, -0.2, 0.7, 0.5, 0.25, -1.5]
+    m.sources = np.array(ent, np.int32)
+    m.source_coef = np.array(coef)
+    return m
+
+
+def test_sweep_layouts(cuda_device):
+    """The sweep step over its settings (CTAs per multiprocessor, velocity lag) and the
+    autotuner's pick: every layout gives the oracle's bits."""
+    m = sweep_case()
+    ref = O.run(m, 24)
+    for per_sm, lag, pf in ((1, 3, 0), (2, 4, 2), (3, 5, 4), (4, 3, 6), (2, 16, 32)):
+        with Solver.from_model(m, fused=F.STEP_SWEEP, graph_steps=6) as s:
+            s.set_sweep(per_sm, lag, pf)
+            s.run(24)
+            assert s.sweep_layout()[:3] == (per_sm, lag, pf)
+            assert s.sweep_layout()[3] > 32
+            got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+        assert_bitwise(got, ref, f"ctas/SM {per_sm} lag {lag}")
+    with Solver.from_model(m, fused=F.STEP_SWEEP) as s:
+        s.autotune(4)
+        s.run(24)
+        got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+    assert_bitwise(got, ref, "autotuned")
+    with Solver.from_model(m) as s, pytest.raises(EwfError) as e:
+        s.set_sweep(2, 3)
+    assert e.value.status == -5
+
+
+def test_sweep_wait_gives_up_and_handle_recovers(cuda_device):
+    """A CTA whose progress is never published (withheld by the diagnostic hook): its neighbours
+    give up after their bounded wait, ewf_run reports the failure instead of hanging, and after
+    a reset the same handle runs bit-exact again."""
+    m = I.random_small(F.MODEL_ORTHO, 64, 48, 24, nt=12, seed=31, damping=F.DAMP_W3D)
+    ref = O.run(m, 12)
+    with Solver.from_model(m, fused=F.STEP_SWEEP, graph_steps=-1) as s:
+        s.sweep_hold(7)
+        with pytest.raises(EwfError) as e:
+            s.run(2)
+        assert e.value.status == -2 and "gave up" in str(e.value)
+        s.sweep_hold(-1)
+        s.reset()
+        s.run(12)
+        got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+    assert_bitwise(got, ref, "after recovery")
+
+
+@pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_SWEEP], ids=["split", "sweep"])
+def test_workload_shapes_small(cuda_device, form):
     """The two benchmark workloads at reduced size, FP32, bit-exact."""
     m = I.iso_homogeneous(n=48, nt=120)
-    assert_bitwise(product(m, 120), O.run(m, 120), "iso48")
+    assert_bitwise(product(m, 120, fused=form), O.run(m, 120), "iso48")
     m = I.ortho_layered(nx=48, ny=48, nz=40, nt=60, src=(24, 24, 4), rec_coords=[4, 20, 40])
-    assert_bitwise(product(m, 60), O.run(m, 60), "ortho48")
+    assert_bitwise(product(m, 60, fused=form), O.run(m, 60), "ortho48")
 
 
 def test_reset_restart_and_checkpoint(cuda_device, tmp_path):

@@ -37,8 +37,9 @@ def edge_mask(q, shape):
 
 def reference(m, nsteps, variant):
     vd = getattr(m, "vdamp", 0.0)
-    assert R.available(m.model, variant, vd, m.damping), \
-        f"missing {R.cubin(m.model, variant, vd, m.damping)}: run oracle/build.py where the reference is"
+    sc = (m.meta or {}).get("scheme")
+    assert R.available(m.model, variant, vd, m.damping, sc), \
+        f"missing {R.cubin(m.model, variant, vd, m.damping, sc)}: run oracle/build.py where the reference is"
     r = R.RefRunner(m, variant)
     try:
         r.run(nsteps)
@@ -75,12 +76,63 @@ def dcq_case(nx=36, ny=40, nz=26, nt=60, seed=25, zs=8):
     return m
 
 
+# the built-in source of the DC_Earthquake FULL family: sigma_xz += 1.0 Src, sigma_yz += 0.8 Src
+FULL_FAMILY_MT = np.array([0.0, 0.0, 0.0, 0.0, 1.0, 0.8])
+
+
+def ok3_case(nx=40, ny=44, nz=24, nt=60, seed=27, zs=9):
+    """The diff_BC2_OK3 scheme: OK4 without BC1 and with a shear modulus of 1e-5 on plane 1."""
+    m = I.random_small(F.MODEL_ISO, nx, ny, nz, nt=nt, seed=seed)
+    m.free_surface = F.FS_NONE
+    m.surface_mu = 1e-5
+    m.set_moment_tensor(FULL_FAMILY_MT, nx // 2 - 3, ny // 2 - 3, zs, 0)
+    m.meta = dict(m.meta or {}, scheme="ok3")
+    return m
+
+
+def constant_moduli(m, c66, c55, c44, b, plane1=None):
+    """The 9 km scheme's fields filled the way the FULL family's scalars act: constant edge shear
+    moduli (plane1: one value on plane k = 1 for all three) and constant buoyancy."""
+    for fid, v in ((F.M_C66XY, c66), (F.M_C55XZ, c55), (F.M_C44YZ, c44)):
+        a = np.full(F.shape(fid, m.nx, m.ny, m.nz), v, np.float32)
+        if plane1 is not None:
+            a[1] = plane1
+        m.materials[fid] = a
+    for fid in (F.M_BX, F.M_BY, F.M_BZ):
+        m.materials[fid] = np.full(F.shape(fid, m.nx, m.ny, m.nz), b, np.float32)
+    return m
+
+
+def ok2_case(nx=36, ny=40, nz=26, nt=60, seed=28, zs=8):
+    """The diff_BC_OK2 scheme: the 3-D-weight form with scalar moduli, no BC1, 1e-5 on plane 1."""
+    m = I.random_small(F.MODEL_ISO_HET, nx, ny, nz, nt=nt, seed=seed, damping=F.DAMP_W3D)
+    mu = float(np.float32(np.median(m.materials[F.M_C66XY][m.materials[F.M_C66XY] > 0])))
+    constant_moduli(m, mu, mu, mu, float(np.float32(1 / 2500.0)), plane1=1e-5)
+    m.free_surface = F.FS_NONE
+    m.set_moment_tensor(FULL_FAMILY_MT, nx // 2 - 3, ny // 2 - 3, zs, 0)
+    m.meta = dict(m.meta or {}, scheme="ok2")
+    return m
+
+
+def full_case(nx=36, ny=40, nz=26, nt=60, seed=29, zs=8):
+    """The FULL scheme: the 3-D-weight form with scalar c66 / c55 / c44, BC1, source kernel after it."""
+    m = I.random_small(F.MODEL_ISO_HET, nx, ny, nz, nt=nt, seed=seed, damping=F.DAMP_W3D, src_order=F.SRC_AFTER_BC1)
+    mu = float(np.median(m.materials[F.M_C66XY][m.materials[F.M_C66XY] > 0]))
+    constant_moduli(m, float(np.float32(mu)), float(np.float32(0.9 * mu)), float(np.float32(1.1 * mu)),
+                    float(np.float32(1 / 2600.0)))
+    m.set_moment_tensor(FULL_FAMILY_MT, nx // 2 - 3, ny // 2 - 3, zs, 0)
+    m.meta = dict(m.meta or {}, scheme="full")
+    return m
+
+
 @pytest.mark.parametrize("make", [iso_case, ortho_case, lambda: iso_case(zs=1), lambda: ortho_case(zs=0),
                                   lambda: ortho_case(damping=F.DAMP_SEPARABLE), isohet_case,
                                   lambda: isohet_case(zs=0, damping=F.DAMP_SEPARABLE), lambda: isohet_case(vdamp=True),
-                                  dcq_case, lambda: dcq_case(zs=1)],
+                                  dcq_case, lambda: dcq_case(zs=1), ok3_case, lambda: ok3_case(zs=0), ok2_case,
+                                  lambda: ok2_case(zs=0), full_case, lambda: full_case(zs=0)],
                          ids=["iso", "ortho", "iso-surface-src", "ortho-surface-src", "ortho-separable", "iso9km",
-                              "iso9km-surface-separable", "iso16km", "dcq", "dcq-surface-src"])
+                              "iso9km-surface-separable", "iso16km", "dcq", "dcq-surface-src", "ok3-no-bc1",
+                              "ok3-surface-src", "ok2-no-bc1", "ok2-surface-src", "full", "full-surface-src"])
 def test_product_bitwise_vs_reference_exact(cuda_device, make):
     m = make()
     rf, rt = reference(m, m.nt, "exact")
@@ -97,7 +149,8 @@ def test_product_bitwise_vs_reference_exact(cuda_device, make):
     assert np.abs(rt).max() > 0
 
 
-@pytest.mark.parametrize("model", [F.MODEL_ISO, F.MODEL_ORTHO, F.MODEL_ISO_HET, -1], ids=["iso", "ortho", "iso16km", "dcq"])
+@pytest.mark.parametrize("model", [F.MODEL_ISO, F.MODEL_ORTHO, F.MODEL_ISO_HET, -1, -2, -3],
+                         ids=["iso", "ortho", "iso16km", "dcq", "ok3", "ok2"])
 def test_seismograms_vs_reference_stock_build(cuda_device, model):
     """North-star criterion: relative L2 seismogram error <= 1e-4 against the reference built with
     its own flags (FMA contraction on), after the full run."""
@@ -111,8 +164,12 @@ def test_seismograms_vs_reference_stock_build(cuda_device, model):
         m.set_moment_tensor(np.array(F.ANISO_LEGACY_MT), 31, 31, 11, 1)
     elif model == F.MODEL_ISO_HET:
         m = isohet_case(nx=64, ny=64, nz=48, nt=400, seed=24, zs=11, vdamp=True)
-    else:
+    elif model == -1:
         m = dcq_case(nx=64, ny=64, nz=48, nt=400, seed=26, zs=11)
+    elif model == -2:
+        m = ok3_case(nx=64, ny=64, nz=48, nt=400, seed=30, zs=11)
+    else:
+        m = ok2_case(nx=64, ny=64, nz=48, nt=400, seed=31, zs=11)
     _, rt = reference(m, m.nt, "stock")
     with Solver.from_model(m) as s:
         s.run(m.nt)

@@ -222,3 +222,49 @@ def test_percomp_weights_follow_the_driver():
     assert np.all(w[F.D_PYZ] == w[F.D_PYZ][:, :, :1])                     # constant along x
     with pytest.raises(ValueError):
         I.percomp_weights(12, 12, 12, dt, lpml=6)
+
+
+def _loop_isotropic_driver_stf(nt, nx, lx):
+    """FINAL.m:372-395 as scalar loops: the x grid, the Gaussian, the shifted copy."""
+    dx = lx / (nx - 1)
+    init = [3.3 * 2e9 * math.exp(-((-lx / 2 + m * dx) / 350.0) ** 2) for m in range(nx)]
+    src = [0.0] * nt
+    for n in range(nx - 199):
+        src[n] = init[n + 199]
+    return src
+
+
+def _loop_orthorhombic_driver_stf(nt, dx, dur=400):
+    """ANIS.m:522-533 as scalar loops: the grid, the Gaussian, minus its second difference,
+    normalised to a peak of 2.5e-3."""
+    npts = int(math.floor(dur * 40.0 / dx * (1 + 4 * 2.0 ** -52))) + 1
+    init = [2.5e-3 * math.exp(-((-dur * 20.0 + m * dx) / 1000.0 / 2) ** 2) for m in range(npts)]
+    g = [-1e9 * ((init[m + 2] - init[m + 1]) - (init[m + 1] - init[m])) for m in range(npts - 2)]
+    src = [0.0] * nt
+    for n, v in enumerate(g):
+        src[n] = v
+    mx = max(src)
+    return [v / mx * 2.5e-3 for v in src]
+
+
+def test_driver_source_time_functions():
+    # the isotropic driver's grid: nx = 64 * NBX = 768, Lx = 7680 m, nt = 3000; Src peaks at 6.6e9
+    nt, nx, lx = 3000, 768, 7680.0
+    a = I.stf_isotropic_driver(nt, nx, lx)
+    b = np.array(_loop_isotropic_driver_stf(nt, nx, lx))
+    assert a.shape == (nt,)
+    np.testing.assert_allclose(a, b, rtol=1e-13, atol=0)
+    np.testing.assert_array_equal(a.astype(np.float32), b.astype(np.float32))
+    assert np.isclose(a.max(), 6.6e9, rtol=1e-3) and a[nx - 199:].max() == 0.0
+    # the orthorhombic driver: dx = 15360 / 767, 2 * 400 - 3 = 797 samples, peak 2.5e-3
+    dx = 2 * 7680 / (768 - 1)
+    a = I.stf_orthorhombic_driver(4500, dx)
+    b = np.array(_loop_orthorhombic_driver_stf(4500, dx))
+    np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-18)
+    np.testing.assert_array_equal(a.astype(np.float32)[a != 0].size, 797)
+    assert a.max() == 2.5e-3 and a[797:].max() == 0.0
+    assert a[398] == a.max() and a[0] < 0 and a[200] < 0     # Ricker-like: central peak, negative lobes
+    with pytest.raises(ValueError):
+        I.stf_orthorhombic_driver(4500, 25.0)                  # 641 points: MATLAB's dimension error
+    with pytest.raises(ValueError):
+        I.stf_isotropic_driver(500, nx, lx)
