@@ -261,7 +261,8 @@ def extra_iso(form: int) -> dict:
 
     m, desc = workload("iso", 0, "")
     with Solver.from_model(m, fused=form) as s:
-        s.autotune(20)
+        kchunk = s.autotune(20)
+        tile = s.tile() if form == F.STEP_SPLIT else None
         s.reset()
         s.run(m.nt)
         ms = []
@@ -272,6 +273,7 @@ def extra_iso(form: int) -> dict:
     value = m.cells * m.nt / (best * 1e-3) / 1e9
     peak, kind = peaks()
     return {"workload": desc, "value": round(value, 3), "unit": UNIT, "ms_per_run": round(best, 3), "runs": len(ms),
+            "kchunk_autotuned": kchunk, **({"tile_y_autotuned": tile} if tile else {}),
             "step_roofline": {"bytes_per_cell": STEP_BYTES["iso"], "achieved": round(value * STEP_BYTES["iso"], 1),
                               "peak": peak, "unit": "GB/s", "frac": round(value * STEP_BYTES["iso"] / peak, 4),
                               "peak_kind": kind},
@@ -401,6 +403,7 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": nt, "receivers": len(m.receivers),
                    "kchunk_autotuned": kchunk, "step": args.step,
+                   **({"tile_y_autotuned": s.tile()} if form == F.STEP_SPLIT else {}),
                    **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {}),
                    **({"sweep_layout": dict(zip(("ctas_per_sm", "lag", "l2_prefetch", "ctas"), s.sweep_layout()))}
                       if form == F.STEP_SWEEP else {}),

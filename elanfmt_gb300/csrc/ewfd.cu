@@ -235,6 +235,7 @@ struct ewf_handle {
     bool graph_dirty = true;
     float last_ms = 0.f;
     int kchunk = 32;
+    int ty = TY;        // two-kernel step: CTA tile height in rows (autotuned)
     bool fdiv = false;  // div_spacing verified for (float) dx, dy, dz
     struct Snapshots *snap = nullptr;  // queued snapshot writer (created on first use)
 };
@@ -968,8 +969,8 @@ extern "C" int ewf_reset(ewf_handle *h)
 template <typename T, int MODEL, int DAMP, bool KAHAN>
 static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t *ev)
 {
-    const dim3 blk(TX, TY);
-    const dim3 grd((h->p.nx + TX - 1) / TX, (h->p.ny + TY - 1) / TY, (h->p.nz + a.kchunk - 1) / a.kchunk);
+    const dim3 blk(TX, h->ty);
+    const dim3 grd((h->p.nx + TX - 1) / TX, (h->p.ny + h->ty - 1) / h->ty, (h->p.nz + a.kchunk - 1) / a.kchunk);
     if (ev) cudaEventRecord(ev[0], h->stream);
     k_stress<T, MODEL, DAMP><<<grd, blk, 0, h->stream>>>(a);
     if (ev) cudaEventRecord(ev[1], h->stream);
@@ -1550,29 +1551,39 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
         if (kchunk) *kchunk = h->kchunk;
         return ewf_reset(h);
     }
-    int best_k = h->kchunk, best_lag = h->wave_lag_pct;
+    int best_k = h->kchunk, best_lag = h->wave_lag_pct, best_ty = h->ty;
     // wavefront step: slabs of 4..16 planes x lag (100000: every stress item before the first velocity item)
     static const int lag_pct[] = {50, 100, 200, 100000};
     const int nvar = h->wave ? 4 : 1;
-    for (int kc : cand) {
-        if (kc > h->p.nz && kc != cand[0]) continue;
-        if (h->wave && kc > 16) continue;
-        for (int vi = 0; vi < nvar; ++vi) {
-            h->kchunk = std::max(4, std::min(kc, h->p.nz));
-            if (h->wave) {
-                h->wave_lag_pct = lag_pct[vi];
-                h->graph_dirty = true;
-            }
-            float ms = 0.f;
-            if ((st = time_setting(h, steps, &ms))) return st;
-            if (ms >= 0.f && ms < best) {
-                best = ms;
-                best_k = h->kchunk;
-                best_lag = h->wave_lag_pct;
+    // two-kernel step: z-chunk x tile height (rows of 32 columns per CTA)
+    const bool split = !h->wave && !h->fused;
+    static const int ty_cand[] = {4, 8, 16};
+    for (int ty : ty_cand) {
+        if (!split && ty != h->ty) continue;
+        if (ty > (h->esz == 4 ? SPLIT_MAX_TY : TY)) continue;
+        for (int kc : cand) {
+            if (kc > h->p.nz && kc != cand[0]) continue;
+            if (h->wave && kc > 16) continue;
+            for (int vi = 0; vi < nvar; ++vi) {
+                h->kchunk = std::max(4, std::min(kc, h->p.nz));
+                h->ty = ty;
+                if (h->wave) {
+                    h->wave_lag_pct = lag_pct[vi];
+                    h->graph_dirty = true;
+                }
+                float ms = 0.f;
+                if ((st = time_setting(h, steps, &ms))) return st;
+                if (ms >= 0.f && ms < best) {
+                    best = ms;
+                    best_k = h->kchunk;
+                    best_lag = h->wave_lag_pct;
+                    best_ty = h->ty;
+                }
             }
         }
     }
     h->kchunk = best_k;
+    h->ty = best_ty;
     h->wave_lag_pct = best_lag;
     h->graph_dirty = true;
     if (kchunk) *kchunk = best_k;
@@ -1612,6 +1623,25 @@ extern "C" int ewf_sweep_hold(ewf_handle *h, int32_t cta)
     if (cta < -1) return ewf_fail(EWF_ERR_ARG, "cta must be >= -1");
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaMemcpy(&h->d_sctl->hold, &cta, sizeof(int), cudaMemcpyHostToDevice));
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_tile(ewf_handle *h, int32_t tile_y)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (h->wave || h->fused || h->sweep) return ewf_fail(EWF_ERR_STATE, "the tile height applies to the two-kernel step");
+    const int mx = h->esz == 4 ? SPLIT_MAX_TY : TY;
+    if (tile_y < 1 || tile_y > mx || (tile_y & (tile_y - 1)))
+        return ewf_fail(EWF_ERR_ARG, "tile_y must be a power of two in [1, %d] (got %d)", mx, tile_y);
+    h->ty = tile_y;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_tile(const ewf_handle *h, int32_t *tile_y)
+{
+    if (!h || !tile_y) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *tile_y = h->ty;
     return EWF_OK;
 }
 

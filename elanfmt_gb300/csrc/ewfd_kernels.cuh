@@ -331,11 +331,20 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
     }
 }
 
+// The two-kernel step's CTAs are TX x blockDim.y columns: blockDim.y (the tile height, chosen by
+// the autotuner) is at most SPLIT_MAX_TY for FP32 and TY for FP64.  The bounds keep the
+// register budget of 4 CTAs of 32 x 8 columns per SM in FP32 (64 per thread) for every height.
+constexpr int SPLIT_MAX_TY = 16;
+template <typename T>
+constexpr int split_max_threads() { return sizeof(T) == 4 ? TX * SPLIT_MAX_TY : TX * TY; }
+template <typename T>
+constexpr int split_min_ctas() { return sizeof(T) == 4 ? 2 : 1; }
+
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY, sizeof(T) == 4 ? 4 : 1) k_stress(const StepArgs<T> a)
+__global__ void __launch_bounds__(split_max_threads<T>(), split_min_ctas<T>()) k_stress(const StepArgs<T> a)
 {
     const int k0 = blockIdx.z * a.kchunk;
-    stress_column<T, MODEL, DAMP, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+    stress_column<T, MODEL, DAMP, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, k0,
                                   min(k0 + a.kchunk, a.nz));
 }
 
@@ -565,11 +574,11 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
 }
 
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-__global__ void __launch_bounds__(TX * TY) k_velocity(const StepArgs<T> a)
+__global__ void __launch_bounds__(split_max_threads<T>()) k_velocity(const StepArgs<T> a)
 {
     const int k0 = blockIdx.z * a.kchunk;
-    velocity_column<T, MODEL, DAMP, KAHAN, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
-                                           min(k0 + a.kchunk, a.nz));
+    velocity_column<T, MODEL, DAMP, KAHAN, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y,
+                                           k0, min(k0 + a.kchunk, a.nz));
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -119,15 +119,28 @@ __device__ __forceinline__ void sweep_prefetch_plane(const SweepArgs<T> &sa, con
     }
 }
 
-// named CTA barriers (ids 1-4; 0 is __syncthreads): arrive without waiting / arrive and wait
-__device__ __forceinline__ void bar_arrive(int id, int count)
+// named CTA barriers (ids 1-6; 0 is __syncthreads): arrive without waiting / arrive and wait.
+// The id is an immediate in each instruction: with an id in a register the assembler has to
+// reserve all sixteen barriers of the CTA, which limits how many CTAs an SM takes.
+template <int ID>
+__device__ __forceinline__ void bar_op(bool wait, int count)
 {
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+    if (wait) asm volatile("bar.sync %0, %1;" ::"n"(ID), "r"(count) : "memory");
+    else asm volatile("bar.arrive %0, %1;" ::"n"(ID), "r"(count) : "memory");
 }
-__device__ __forceinline__ void bar_sync(int id, int count)
+__device__ __forceinline__ void bar_id(int id, bool wait, int count)
 {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+    switch (id) {
+        case 1: bar_op<1>(wait, count); break;
+        case 2: bar_op<2>(wait, count); break;
+        case 3: bar_op<3>(wait, count); break;
+        case 4: bar_op<4>(wait, count); break;
+        case 5: bar_op<5>(wait, count); break;
+        default: bar_op<6>(wait, count); break;
+    }
 }
+__device__ __forceinline__ void bar_arrive(int id, int count) { bar_id(id, false, count); }
+__device__ __forceinline__ void bar_sync(int id, int count) { bar_id(id, true, count); }
 __device__ __forceinline__ int bar_stored(int p) { return 1 + (p & 1); }
 // grants run SWEEP_GRANT = 2 iterations ahead, so up to three "cleared" phases can be open at
 // once (four ids); "stored" has at most two open

@@ -76,6 +76,8 @@ SIGNATURES = {
     "ewf_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ewf_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_wave_hold": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     "ewf_get_sweep": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
@@ -280,10 +282,20 @@ class Solver:
         return dict(zip(("stress", "inject", "velocity", "record"), list(out)))
 
     def autotune(self, nsteps: int = 30) -> int:
-        """Picks the fastest z-chunk by timing `nsteps` steps per candidate; resets the state."""
+        """Picks the fastest z-chunk (and, for the two-kernel step, tile height) by timing `nsteps`
+        steps per candidate; resets the state.  Returns the z-chunk."""
         k = C.c_int32()
         _check(self._lib.ewf_autotune(self._h, int(nsteps), C.byref(k)), "ewf_autotune")
         return k.value
+
+    def set_tile(self, tile_y: int) -> None:
+        """Two-kernel step: CTA tile height in rows of 32 columns (results do not depend on it)."""
+        _check(self._lib.ewf_set_tile(self._h, int(tile_y)), "ewf_set_tile")
+
+    def tile(self) -> int:
+        ty = C.c_int32()
+        _check(self._lib.ewf_get_tile(self._h, C.byref(ty)), "ewf_get_tile")
+        return ty.value
 
     def set_wave(self, lag_pct: int) -> None:
         """Wavefront step: lag of the velocity items behind the stress items, percent of the resident

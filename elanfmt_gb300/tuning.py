@@ -1,13 +1,18 @@
-"""Cache of the z-chunk autotuner's choices (JSON), so a workload is timed once per GPU model.
+"""Cache of the autotuner's choices (JSON), so a workload is timed once per GPU model.
 
 The library's autotuner (`ewf_autotune`, `ewf_batch_autotune`) times the step for z-chunks of
-4..64 planes.  The best chunk depends on the GPU, the scheme (model, damping, precision, step
-form) and the grid, not on the inputs' values, so it is stored under that key (the wavefront
-form's lag is re-tuned by `ewf_autotune` when a handle needs it):
+4..64 planes and, for the two-kernel step, CTA tile heights of 4, 8 and 16 rows.  The best
+setting depends on the GPU, the scheme (model, damping, precision, step form) and the grid, not
+on the inputs' values, so it is stored under that key (the wavefront form's lag is re-tuned by
+`ewf_autotune` when a handle needs it):
 
     from elanfmt_gb300 import tuning
     k = tuning.kchunk_for(model, precision=F.PREC_F32)      # cached, or tuned once and stored
     with Solver.from_model(model, kchunk=k) as s: ...
+
+    k, ty = tuning.split_setting_for(model)                 # z-chunk and tile height
+    with Solver.from_model(model, kchunk=k) as s:
+        s.set_tile(ty)
 
 The cache file defaults to $EWF_TUNING_CACHE or ~/.cache/elanfmt_gb300/kchunk.json.
 """
@@ -43,11 +48,12 @@ def load(path: str | None = None) -> dict:
         return {}
 
 
-def store(k: str, kchunk: int, path: str | None = None) -> None:
-    """Adds one entry; the file is replaced atomically so concurrent writers never leave it torn."""
+def store(k: str, value, path: str | None = None) -> None:
+    """Adds one entry (an int, or a list of ints); the file is replaced atomically so concurrent
+    writers never leave it torn."""
     p = path or cache_path()
     data = load(p)
-    data[k] = int(kchunk)
+    data[k] = [int(v) for v in value] if isinstance(value, (list, tuple)) else int(value)
     os.makedirs(os.path.dirname(p) or ".", exist_ok=True)
     fd, tmp = tempfile.mkstemp(dir=os.path.dirname(p) or ".", suffix=".tmp")
     with os.fdopen(fd, "w") as fh:
@@ -78,3 +84,29 @@ def kchunk_for(m, precision: int = F.PREC_F32, fused: int = F.STEP_SPLIT, nsteps
     best = int(tune(m, precision, fused, nsteps))
     store(k, best, path)
     return best
+
+
+def split_setting_for(m, precision: int = F.PREC_F32, nsteps: int = 30, path: str | None = None,
+                      device_name: str | None = None, tune=None) -> tuple[int, int]:
+    """The two-kernel step's cached (z-chunk, tile height) for this workload shape, or the
+    autotuner's choice (then cached).  `tune(m, precision, nsteps) -> (kchunk, tile_y)` replaces
+    the GPU autotuner (tests)."""
+    if device_name is None:
+        import torch
+
+        device_name = torch.cuda.get_device_name()
+    k = key(device_name, m, precision, F.STEP_SPLIT) + "|tile"
+    data = load(path)
+    v = data.get(k)
+    if isinstance(v, list) and len(v) == 2:
+        return int(v[0]), int(v[1])
+    if tune is None:
+        from .solver import Solver
+
+        def tune(m_, p_, n_):
+            with Solver.from_model(m_, precision=p_) as s:
+                return s.autotune(n_), s.tile()
+
+    kc, ty = (int(x) for x in tune(m, precision, nsteps))
+    store(k, [kc, ty], path)
+    return kc, ty

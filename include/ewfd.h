@@ -213,10 +213,17 @@ int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4]);
 int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
 
 /* Autotuner: times `nsteps` steps for each z-chunk candidate (planes per CTA) with CUDA events,
- * keeps the fastest (returned in *kchunk, may be NULL) and resets the state.  The wavefront
- * step also tunes its lag (kept in the handle); the sweep step tunes its CTAs per
- * multiprocessor and its lag instead of the z-chunk. */
+ * keeps the fastest (returned in *kchunk, may be NULL) and resets the state.  The two-kernel step
+ * also tunes its tile height (4, 8, 16 rows; ewf_get_tile), the wavefront step its lag (both kept
+ * in the handle); the sweep step tunes its CTAs per multiprocessor, lag and prefetch distance
+ * instead of the z-chunk. */
 int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
+
+/* Two-kernel step (fused = EWF_STEP_SPLIT): the height of a CTA's tile in rows of 32 columns
+ * (a power of two, 1..16 in FP32, 1..8 in FP64; default 8), set by ewf_autotune together with the
+ * z-chunk; results do not depend on it.  ewf_set_tile: EWF_ERR_STATE for the other step forms. */
+int ewf_set_tile(ewf_handle *h, int32_t tile_y);
+int ewf_get_tile(const ewf_handle *h, int32_t *tile_y);
 
 /* Wavefront step (fused = EWF_STEP_WAVE): the lag of the velocity items behind the stress items
  * in percent of the resident CTAs, 1..100000 (set by ewf_autotune; results do not depend on it).

@@ -244,6 +244,43 @@ def test_wave_wait_gives_up_and_handle_recovers(cuda_device):
     assert_bitwise(got, ref, "after recovery")
 
 
+@pytest.mark.parametrize("prec", [F.PREC_F32, F.PREC_F32_KAHAN, F.PREC_F64], ids=["f32", "kahan", "f64"])
+def test_split_tile_heights(cuda_device, prec):
+    """The two-kernel step over its CTA tile heights (rows of 32 columns) and the autotuner's
+    pick of z-chunk and height: every setting gives the oracle's bits, on grids whose extents
+    are not multiples of the tile."""
+    heights = (1, 2, 4, 8, 16) if prec != F.PREC_F64 else (1, 2, 4, 8)
+    for model, damping, shape in ((F.MODEL_ORTHO, F.DAMP_SEPARABLE, (35, 37, 21)), (F.MODEL_ISO, None, (33, 19, 17))):
+        m = I.random_small(model, *shape, nt=20, seed=53, damping=damping)
+        ref = O.run(m, 20, prec)
+        dt = np.float64 if prec == F.PREC_F64 else np.float32
+        for ty in heights:
+            with Solver.from_model(m, precision=prec, kchunk=6, graph_steps=4) as s:
+                s.set_tile(ty)
+                assert s.tile() == ty
+                s.run(20)
+                got = ([s.field(q, dt) for q in F.STATE], s.seismograms())
+            assert_bitwise(got, ref, f"model {model} tile height {ty}")
+        with Solver.from_model(m, precision=prec) as s:
+            s.autotune(3)
+            assert s.tile() in (4, 8, 16)
+            s.run(20)
+            got = ([s.field(q, dt) for q in F.STATE], s.seismograms())
+        assert_bitwise(got, ref, f"model {model} autotuned")
+    m = I.random_small(F.MODEL_ORTHO, 24, 24, 16, nt=4, seed=3, damping=F.DAMP_W3D)
+    with Solver.from_model(m, precision=prec) as s:
+        for bad in (0, 3, 32):
+            with pytest.raises(EwfError) as e:
+                s.set_tile(bad)
+            assert e.value.status == -1
+        if prec == F.PREC_F64:
+            with pytest.raises(EwfError):
+                s.set_tile(16)
+    with Solver.from_model(m, fused=F.STEP_WAVE) as s, pytest.raises(EwfError) as e:
+        s.set_tile(4)
+    assert e.value.status == -5
+
+
 def sweep_case():
     """A grid of a few hundred sweep CTAs with point sources on CTA-range borders, on several
     entries of one cell, and on cells the stress pass never updates (sxy at i = nx and at i = 0,

@@ -33,3 +33,23 @@ def test_unreadable_cache_is_empty(tmp_path):
     assert tuning.load(str(p)) == {}
     tuning.store("k", 8, str(p))
     assert tuning.load(str(p)) == {"k": 8}
+
+
+def test_split_setting_cached_with_tile_height(tmp_path):
+    path = str(tmp_path / "k.json")
+    calls = []
+
+    def fake(m, prec, n):
+        calls.append((m.nx, prec))
+        return (8, 16) if m.nx == 20 else (24, 4)
+
+    a = I.random_small(F.MODEL_ORTHO, 20, 18, 16, nt=5, seed=1)
+    b = I.random_small(F.MODEL_ISO, 24, 18, 16, nt=5, seed=1)
+    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16)
+    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16)
+    assert tuning.split_setting_for(b, path=path, device_name="gpuX", tune=fake) == (24, 4)
+    assert len(calls) == 2
+    # the z-chunk-only entries of the same shape stay separate
+    assert tuning.kchunk_for(a, path=path, device_name="gpuX", tune=lambda *x: 12) == 12
+    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16)
+    assert sorted(len(v) if isinstance(v, list) else 1 for v in tuning.load(path).values()) == [1, 2, 2]
