@@ -59,6 +59,7 @@ struct Family {
     int *d_item0 = nullptr;
     int nitems = 0;
     int grid_stress = 0, grid_vel = 0;
+    int ty = TY;                  // CTA tile height of the family's launches
 };
 
 float *bptr(const Prob &q, void *alloc) { return alloc ? (float *)alloc + q.base_off : nullptr; }
@@ -96,6 +97,7 @@ struct ewf_batch {
     void *d_stage = nullptr;
     size_t stage_bytes = 0;
     bool dirty = true;   // device tables need a rebuild
+    int ty = TY;         // CTA tile height in rows of 32 columns (autotuned; 4, 8 or 16)
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 64;
     float last_ms = 0.f;
@@ -357,35 +359,37 @@ extern "C" int ewf_batch_set_receivers(ewf_batch *b, int32_t prob, int32_t n, co
 }
 
 template <typename K>
-static int persistent_grid(K kernel, int sms, int nitems)
+static int persistent_grid(K kernel, int sms, int nitems, int ty)
 {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TX * TY, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TX * ty, 0);
     return std::max(1, std::min(nitems, sms * std::max(1, per_sm)));
 }
 
 template <int MODEL, int DAMP>
-static int family_grid_t(bool stress, int sms, int items)
+static int family_grid_t(bool stress, int sms, int items, int ty)
 {
-    return stress ? persistent_grid(k_bstress<float, MODEL, DAMP>, sms, items)
-                  : persistent_grid(k_bvelocity<float, MODEL, DAMP>, sms, items);
+    return stress ? persistent_grid(k_bstress<float, MODEL, DAMP>, sms, items, ty)
+                  : persistent_grid(k_bvelocity<float, MODEL, DAMP>, sms, items, ty);
 }
 
 template <bool STRESS>
 static int family_grid(const Family &f, int sms, int items)
 {
-    if (f.model == EWF_MODEL_ISO) return family_grid_t<MODEL_ISO, DAMP_PML1D>(STRESS, sms, items);
-    if (f.damping == EWF_DAMP_W3D) return family_grid_t<MODEL_ORTHO, DAMP_W3D>(STRESS, sms, items);
-    return family_grid_t<MODEL_ORTHO, DAMP_SEP>(STRESS, sms, items);
+    if (f.model == EWF_MODEL_ISO) return family_grid_t<MODEL_ISO, DAMP_PML1D>(STRESS, sms, items, f.ty);
+    if (f.damping == EWF_DAMP_W3D) return family_grid_t<MODEL_ORTHO, DAMP_W3D>(STRESS, sms, items, f.ty);
+    return family_grid_t<MODEL_ORTHO, DAMP_SEP>(STRESS, sms, items, f.ty);
 }
 
 template <int MODEL, int DAMP>
 static void launch_family_t(const Family &f, bool stress, cudaStream_t s)
 {
     if (stress)
-        k_bstress<float, MODEL, DAMP><<<f.grid_stress, dim3(TX, TY), 0, s>>>(f.d_probs, f.d_item0, (int)f.probs.size(), f.nitems);
+        k_bstress<float, MODEL, DAMP><<<f.grid_stress, dim3(TX, f.ty), 0, s>>>(f.d_probs, f.d_item0, (int)f.probs.size(),
+                                                                               f.nitems);
     else
-        k_bvelocity<float, MODEL, DAMP><<<f.grid_vel, dim3(TX, TY), 0, s>>>(f.d_probs, f.d_item0, (int)f.probs.size(), f.nitems);
+        k_bvelocity<float, MODEL, DAMP><<<f.grid_vel, dim3(TX, f.ty), 0, s>>>(f.d_probs, f.d_item0, (int)f.probs.size(),
+                                                                              f.nitems);
 }
 
 static void launch_family(const Family &f, bool stress, cudaStream_t s)
@@ -433,7 +437,7 @@ static int build_tables(ewf_batch *b)
         d.smu_on = p.surface_mu > 0.0 ? 1 : 0;
         d.smu = (float)p.surface_mu;
         bp.tiles_x = (p.nx + TX - 1) / TX;
-        bp.tiles_y = (p.ny + TY - 1) / TY;
+        bp.tiles_y = (p.ny + b->ty - 1) / b->ty;
         bp.chunks = (p.nz + q.kchunk - 1) / q.kchunk;
     }
     // families (single-RHS problems sharing one persistent launch) and their work lists;
@@ -450,6 +454,7 @@ static int build_tables(ewf_batch *b)
         if (!fam_of.count(key)) {
             fam_of[key] = (int)b->fams.size();
             b->fams.push_back(Family{key.first, key.second});
+            b->fams.back().ty = b->ty;
         }
         b->fams[fam_of[key]].probs.push_back(i);
     }
@@ -545,22 +550,22 @@ static int build_tables(ewf_batch *b)
 }
 
 template <int MODEL, int DAMP>
-static void launch_mr_t(const BatchProb<float> &p, bool stress, cudaStream_t s)
+static void launch_mr_t(const BatchProb<float> &p, int ty, bool stress, cudaStream_t s)
 {
     const dim3 grd(p.tiles_x * p.R, p.tiles_y, p.chunks);
     if (stress)
-        k_stress_mr<float, MODEL, DAMP><<<grd, dim3(TX, TY), 0, s>>>(p.a, p.R, p.rhs_stride);
+        k_stress_mr<float, MODEL, DAMP><<<grd, dim3(TX, ty), 0, s>>>(p.a, p.R, p.rhs_stride);
     else
-        k_velocity_mr<float, MODEL, DAMP><<<grd, dim3(TX, TY), 0, s>>>(p.a, p.R, p.rhs_stride);
+        k_velocity_mr<float, MODEL, DAMP><<<grd, dim3(TX, ty), 0, s>>>(p.a, p.R, p.rhs_stride);
 }
 
 static void launch_mr(const ewf_batch *b, int i, bool stress, cudaStream_t s)
 {
     const ewf_params &q = b->probs[i].p;
     const BatchProb<float> &p = b->h_all[i];
-    if (q.model == EWF_MODEL_ISO) launch_mr_t<MODEL_ISO, DAMP_PML1D>(p, stress, s);
-    else if (q.damping == EWF_DAMP_W3D) launch_mr_t<MODEL_ORTHO, DAMP_W3D>(p, stress, s);
-    else launch_mr_t<MODEL_ORTHO, DAMP_SEP>(p, stress, s);
+    if (q.model == EWF_MODEL_ISO) launch_mr_t<MODEL_ISO, DAMP_PML1D>(p, b->ty, stress, s);
+    else if (q.damping == EWF_DAMP_W3D) launch_mr_t<MODEL_ORTHO, DAMP_W3D>(p, b->ty, stress, s);
+    else launch_mr_t<MODEL_ORTHO, DAMP_SEP>(p, b->ty, stress, s);
 }
 
 static void batch_step(ewf_batch *b, cudaEvent_t *ev)
@@ -690,18 +695,21 @@ extern "C" int ewf_batch_get_field(ewf_batch *b, int32_t prob, int32_t rhs, int3
     return EWF_OK;
 }
 
-// Times `nsteps` steps for each z-chunk candidate with CUDA events, keeps the fastest, and
-// leaves the batch reset (the tuning steps advance the state).
+// Times `nsteps` steps for each (tile height, z-chunk) candidate with CUDA events, keeps the
+// fastest, and leaves the batch reset (the tuning steps advance the state).
 extern "C" int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk_out)
 {
     if (!b || nsteps < 1) return ewf_fail(EWF_ERR_ARG, "bad argument");
     static const int cand[] = {8, 12, 16, 24, 32, 48, 64};
+    static const int ty_cand[] = {4, 8, 16};
     float best = 1e30f;
-    int best_k = 16;
+    int best_k = 16, best_ty = b->ty;
     cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (int ty : ty_cand)
     for (int kc : cand) {
         for (auto &q : b->probs) q.kchunk = std::max(4, std::min(kc, q.p.nz));
+        b->ty = ty;
         b->dirty = true;
         int st = batch_ready(b);
         if (st) { for (auto &e : ev) cudaEventDestroy(e); return st; }
@@ -714,13 +722,30 @@ extern "C" int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk_
         CK(cudaStreamSynchronize(b->stream));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-        if (ms < best) { best = ms; best_k = kc; }
+        if (ms < best) { best = ms; best_k = kc; best_ty = ty; }
     }
     for (auto &e : ev) cudaEventDestroy(e);
     for (auto &q : b->probs) q.kchunk = std::max(4, std::min(best_k, q.p.nz));
+    b->ty = best_ty;
     b->dirty = true;
     int st = batch_ready(b);
     if (st) return st;
     if (kchunk_out) *kchunk_out = best_k;
     return ewf_batch_reset(b);
+}
+
+extern "C" int ewf_batch_set_tile(ewf_batch *b, int32_t tile_y)
+{
+    if (!b) return ewf_fail(EWF_ERR_ARG, "NULL batch");
+    if (tile_y != 4 && tile_y != 8 && tile_y != 16) return ewf_fail(EWF_ERR_ARG, "tile_y must be 4, 8 or 16 (got %d)", tile_y);
+    b->ty = tile_y;
+    b->dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_batch_get_tile(const ewf_batch *b, int32_t *tile_y)
+{
+    if (!b || !tile_y) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *tile_y = b->ty;
+    return EWF_OK;
 }

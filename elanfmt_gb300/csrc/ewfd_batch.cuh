@@ -25,6 +25,10 @@ struct BatchProb {
     int R, tiles_x, tiles_y, chunks, item0;  // work items of this problem start at item0
 };
 
+// CTAs are TX x blockDim.y columns; blockDim.y (the tile height, autotuned) is one of 4, 8, 16.
+constexpr int BATCH_MIN_TY = 4;
+constexpr int BATCH_MAX_TY = 16;
+
 __device__ __forceinline__ int find_problem(const int *item0, int nprob, int item)
 {
     int lo = 0, hi = nprob - 1;
@@ -50,13 +54,14 @@ __device__ __forceinline__ void item_args(const BatchProb<T> &P, int item, StepA
     const int ty_ = rem % P.tiles_y;
     const int ch = rem / P.tiles_y;
     X = tx_ * TX + threadIdx.x;
-    j = ty_ * TY + threadIdx.y;
+    j = ty_ * (int)blockDim.y + threadIdx.y;
     k0 = ch * P.a.kchunk;
     k1 = min(k0 + P.a.kchunk, P.a.nz);
     __syncthreads();  // the previous item is done with sa
     const int t = threadIdx.y * TX + threadIdx.x;
     constexpr int NW = sizeof(StepArgs<T>) / sizeof(int);
     static_assert(sizeof(StepArgs<T>) % sizeof(int) == 0, "StepArgs is copied as words");
+    static_assert(NW <= TX * BATCH_MIN_TY, "the smallest CTA copies StepArgs in one pass");
     if (t < NW) reinterpret_cast<int *>(&sa)[t] = reinterpret_cast<const int *>(&P.a)[t];
     __syncthreads();
     if (t < 9) sa.f[t] += (long long)r * P.rhs_stride;
@@ -66,7 +71,7 @@ __device__ __forceinline__ void item_args(const BatchProb<T> &P, int item, StepA
 // Stress phase for every problem of one (model, damping) family: a persistent grid striding
 // over the work items.
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY, 4) k_bstress(const BatchProb<T> *__restrict__ probs,
+__global__ void __launch_bounds__(TX * BATCH_MAX_TY, 2) k_bstress(const BatchProb<T> *__restrict__ probs,
                                                          const int *__restrict__ item0, int nprob, int nitems)
 {
     __shared__ StepArgs<T> sa;
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(TX * TY, 4) k_bstress(const BatchProb<T> *__re
 }
 
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY, 4) k_bvelocity(const BatchProb<T> *__restrict__ probs,
+__global__ void __launch_bounds__(TX * BATCH_MAX_TY, 2) k_bvelocity(const BatchProb<T> *__restrict__ probs,
                                                            const int *__restrict__ item0, int nprob, int nitems)
 {
     __shared__ StepArgs<T> sa;
@@ -97,22 +102,22 @@ __global__ void __launch_bounds__(TX * TY, 4) k_bvelocity(const BatchProb<T> *__
 // so the R CTAs of a tile are dispatched together and read the tile's material planes from HBM
 // once (the other R-1 reads hit L2).
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY, 4) k_stress_mr(const StepArgs<T> a, int R, long long rhs_stride)
+__global__ void __launch_bounds__(TX * BATCH_MAX_TY, 2) k_stress_mr(const StepArgs<T> a, int R, long long rhs_stride)
 {
     const int r = blockIdx.x % R;
     const int tx = blockIdx.x / R;
     const int k0 = blockIdx.z * a.kchunk;
-    stress_column<T, MODEL, DAMP, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+    stress_column<T, MODEL, DAMP, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, k0,
                                         min(k0 + a.kchunk, a.nz), (long long)r * rhs_stride);
 }
 
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(TX * TY, 4) k_velocity_mr(const StepArgs<T> a, int R, long long rhs_stride)
+__global__ void __launch_bounds__(TX * BATCH_MAX_TY, 2) k_velocity_mr(const StepArgs<T> a, int R, long long rhs_stride)
 {
     const int r = blockIdx.x % R;
     const int tx = blockIdx.x / R;
     const int k0 = blockIdx.z * a.kchunk;
-    velocity_column<T, MODEL, DAMP, false, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * TY + threadIdx.y, k0,
+    velocity_column<T, MODEL, DAMP, false, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, k0,
                                                  min(k0 + a.kchunk, a.nz), (long long)r * rhs_stride);
 }
 

@@ -98,6 +98,8 @@ SIGNATURES = {
     "ewf_batch_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t,
                                       C.c_int32]),
     "ewf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "ewf_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_batch_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_mlp_gemm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_mlp_status": (C.c_int, []),
@@ -458,6 +460,15 @@ class Batch:
         k = C.c_int32()
         _check(self._lib.ewf_batch_autotune(self._h, int(nsteps), C.byref(k)), "ewf_batch_autotune")
         return k.value
+
+    def set_tile(self, tile_y: int) -> None:
+        """CTA tile height of the batch's launches (4, 8 or 16 rows of 32 columns)."""
+        _check(self._lib.ewf_batch_set_tile(self._h, int(tile_y)), "ewf_batch_set_tile")
+
+    def tile(self) -> int:
+        ty = C.c_int32()
+        _check(self._lib.ewf_batch_get_tile(self._h, C.byref(ty)), "ewf_batch_get_tile")
+        return ty.value
 
     def seismograms(self, prob: int, rhs: int) -> np.ndarray:
         m = self.models[prob]

@@ -256,12 +256,13 @@ _REC_PAIRS = ((F.F_VX, 0, 0, 0), (F.F_VX, 1, 0, 0), (F.F_VY, 0, 0, 0), (F.F_VY, 
               (F.F_VZ, 0, 0, 1))
 
 
-def generate(m, sources: np.ndarray, picks: list, rec_xy: np.ndarray, runs_per_batch: int = 10, log=None):
+def generate(m, sources: np.ndarray, picks: list, rec_xy: np.ndarray, runs_per_batch: int = 10, log=None,
+             decimate: int = 1):
     """Runs the 6 elementary moment tensors for every source cell (xs, ys, zs) with the batched
     solver (one problem whose right-hand sides are 6 per source, each a co-located point source)
-    and returns, per source, the velocity traces [npick, 18, nt] (float32) at the centres of its
-    picked receiver cells (indices into rec_xy, depth cell 1), plus the device seconds per
-    source."""
+    and returns, per source, the velocity traces [npick, 18, nt / decimate] (float32; every
+    `decimate`-th time step) at the centres of its picked receiver cells (indices into rec_xy,
+    depth cell 1), plus the device seconds per source."""
     out = []
     secs = 0.0
     for a in range(0, len(sources), runs_per_batch):
@@ -284,10 +285,10 @@ def generate(m, sources: np.ndarray, picks: list, rec_xy: np.ndarray, runs_per_b
             secs += b.run(m.nt) * 1e-3
             for u, s in enumerate(chunk):
                 sel = np.array([pos[int(r)] for r in picks[s]])
-                tr = np.empty((len(sel), NCOMP, m.nt), np.float32)
+                tr = np.empty((len(sel), NCOMP, len(range(0, m.nt, decimate))), np.float32)
                 for q in range(6):
                     t = b.seismograms(0, 6 * u + q).reshape(len(union), 3, 2, m.nt).mean(axis=2)
-                    tr[:, 3 * q:3 * q + 3, :] = t[sel]
+                    tr[:, 3 * q:3 * q + 3, :] = t[sel][..., ::decimate]
                 out.append(tr)
         if log:
             log(f"generated {chunk[-1] + 1}/{len(sources)} sources")
@@ -295,28 +296,35 @@ def generate(m, sources: np.ndarray, picks: list, rec_xy: np.ndarray, runs_per_b
 
 
 def geometry(m, src: np.ndarray, rec_xy: np.ndarray) -> np.ndarray:
-    """Per (source, receiver): (depth, offset, azimuth, distance) in metres / radians.  The model is
-    laterally homogeneous, so these determine the Green's functions up to the PML's influence."""
+    """Per (source, receiver): (depth, offset, azimuth, distance, source x, source y) in metres /
+    radians.  The model is laterally homogeneous, so the first three determine the Green's
+    functions up to the PML's influence (which the source position carries)."""
     xs, ys, zs = (src[:, None, 0] * m.dx, src[:, None, 1] * m.dy, src[:, None, 2] * m.dz)
     dxr = rec_xy[None, :, 0] * m.dx - xs
     dyr = rec_xy[None, :, 1] * m.dy - ys
     off = np.hypot(dxr, dyr)
     az = np.arctan2(dyr, dxr)
     depth = np.broadcast_to(zs, off.shape)
-    return np.stack([depth, off, az, np.hypot(off, depth)], axis=-1)
+    return np.stack([depth, off, az, np.hypot(off, depth), np.broadcast_to(xs, off.shape),
+                     np.broadcast_to(ys, off.shape)], axis=-1)
 
 
-def features(geo: np.ndarray, structured: bool, az4: bool = False) -> np.ndarray:
+def features(geo: np.ndarray, structured: bool, az4: bool = False, full: bool = False) -> np.ndarray:
     """Network inputs.  structured: (depth, offset) -- the network predicts the fundamental traces,
     which do not depend on azimuth in a laterally homogeneous medium; az4 adds cos 4az, sin 4az,
     the lowest harmonic of a cubic grid's direction-dependent dispersion.  Otherwise (depth,
     offset, cos az, sin az, cos 2az, sin 2az): the radiation patterns of the elementary moment
-    tensors are combinations of the first and second azimuthal harmonics."""
+    tensors are combinations of the first and second azimuthal harmonics; `full` adds the source's
+    x and y (the five inputs source x, y, depth, receiver offset, azimuth, with no symmetry
+    assumed)."""
     depth, off, az = geo[..., 0], geo[..., 1], geo[..., 2]
     if structured:
         cols = [depth, off] + ([np.cos(4 * az), np.sin(4 * az)] if az4 else [])
         return np.stack(cols, axis=-1).astype(np.float32)
-    return np.stack([depth, off, np.cos(az), np.sin(az), np.cos(2 * az), np.sin(2 * az)], axis=-1).astype(np.float32)
+    cols = [depth, off, np.cos(az), np.sin(az), np.cos(2 * az), np.sin(2 * az)]
+    if full:
+        cols = [geo[..., 4], geo[..., 5]] + cols
+    return np.stack(cols, axis=-1).astype(np.float32)
 
 
 NFUND = 10            # fundamental traces of a point moment tensor in a laterally homogeneous medium
@@ -372,12 +380,13 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> np.ndarray:
 
 
 def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: int = 1280, per_run: int = 64,
-                 seed: int = 7, max_offset: float = 12000.0, log=print) -> dict | None:
+                 seed: int = 7, max_offset: float = 12000.0, log=print, f0: float = 0.5, decimate: int = 1,
+                 dx: float = 120.0) -> dict | None:
     """Runs the solver for train_runs + test_runs random source cells (depth 2-8 km, scaled to the
-    grid) and keeps, per source, `per_run` receivers with offsets in 1 km .. max_offset.  Under
-    torch.distributed the sources are shared out over the ranks (elanfmt_gb300.runs) and only
-    rank 0 gets the dataset (None elsewhere)."""
-    m = layered_iso(n=n, nt=nt)
+    grid) for nt time steps and keeps, per source, `per_run` receivers with offsets in 1 km ..
+    max_offset, every `decimate`-th sample.  Under torch.distributed the sources are shared out
+    over the ranks (elanfmt_gb300.runs) and only rank 0 gets the dataset (None elsewhere)."""
+    m = layered_iso(n=n, nt=nt, f0=f0, dx=dx)
     lpml = m.meta["lpml"]
     rec_xy = surface_receivers(n, lpml, 3)
     rng = np.random.default_rng(seed)
@@ -399,7 +408,7 @@ def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: i
     rank, world = (dist.get_rank(), dist.get_world_size()) if dist else (0, 1)
     mine = list(runs.shard(nrun, rank, world))
     t0 = time.perf_counter()
-    local, fdtd_s_per_src = generate(m, src[mine], [picks[s] for s in mine], rec_xy, log=log)
+    local, fdtd_s_per_src = generate(m, src[mine], [picks[s] for s in mine], rec_xy, log=log, decimate=decimate)
     got = runs.gather(dict(zip(mine, local)), dist)
     if got is None:
         return None
@@ -409,6 +418,7 @@ def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: i
     samples_src = np.concatenate([[s] * len(picks[s]) for s in range(nrun)]).astype(np.int64)
     samples_rec = np.concatenate(picks)
     return dict(m=m, rec_xy=rec_xy, src=src, train_runs=train_runs, test_runs=test_runs, per_run=per_run,
+                decimate=decimate, max_offset=max_offset,
                 samples_src=samples_src, geo=geo[samples_src, samples_rec],
                 Y=np.concatenate([t.reshape(len(t), -1) for t in traces]), fdtd_s_per_src=fdtd_s_per_src)
 
@@ -427,7 +437,7 @@ def fourier_features(Xs: np.ndarray, sigma: float, width: int, seed: int = 0) ->
 
 def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 512, layers: int = 4,
                      lr: float = 1e-3, spreading: bool = True, structured: bool = True, fourier: float = 0.0,
-                     az4: bool = False, log=print) -> dict:
+                     az4: bool = False, full: bool = False, log=print) -> dict:
     """Trains the MLP on the training sources of a dataset and scores it on the held-out ones
     against the solver's traces; also scores the nearest-neighbour method (no network) and the
     fallback policy.  structured: the network maps (depth, offset) to the 10 fundamental traces
@@ -448,7 +458,9 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
     live = energy > 1e-3 * np.median(energy)
     test = ~is_train & live
     val_src = val_src & live
-    X = features(geo, structured, az4)
+    if full:
+        structured = False
+    X = features(geo, structured, az4, full)
     mu, sd = X[fit].mean(axis=0), X[fit].std(axis=0) + 1e-6
     Xs = (X - mu) / sd
     # geometric spreading: targets scaled by distance, so that near and far receivers weigh alike
@@ -547,7 +559,9 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
                 "frac_le_1e-2": float((e <= 1e-2).mean()), "frac_le_1e-1": float((e <= 1e-1).mean())}
 
     return {
-        "model": f"layered isotropic {n}^3, dx {m.dx:.0f} m, 8 layers, {nt} steps, Ricker {m.meta['f0']} Hz",
+        "model": f"layered isotropic {n}^3, dx {m.dx:.0f} m, 8 layers, {m.nt} steps recorded every "
+                 f"{ds.get('decimate', 1)} -> {nt} samples, Ricker {m.meta['f0']} Hz, offsets 1 km - "
+                 f"{ds.get('max_offset', 12000.0) / 1000:.0f} km",
         "train_sources": train_runs, "test_sources": ds["test_runs"], "receivers_recorded": int(len(ds["rec_xy"])),
         "queries_per_source": per_run, "train_samples": int(fit.sum()), "val_samples": int(val_src.sum()),
         "test_samples": nq, "test_samples_without_energy": int((~is_train & ~live).sum()),
@@ -556,7 +570,8 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
         "structured": structured,
         "fourier_sigma": fourier, "az4": az4,
         "features": ("depth, offset -> 10 fundamental traces, mixed per azimuth" if structured else
-                     "depth, offset, cos/sin az, cos/sin 2az -> 18 traces") + " (standardised)" +
+                     ("source x, y, " if full else "") + "depth, offset, cos/sin az, cos/sin 2az -> 18 traces")
+                    + " (standardised)" +
                     ("; targets x distance" if spreading else ""),
         "symmetry_floor_rel_l2": stats(sym_err) if structured else None,
         "train_steps": steps, "train_seconds": round(train_s, 2), "loss_first_last": [losses[0][1], losses[-1][1]],
@@ -574,6 +589,44 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
     }
 
 
+def symmetry_floor(f0s=(0.5, 0.35, 0.25), sources: int = 16, n: int = 192, dx: float = 120.0, per_run: int = 64,
+                   max_offset: float = 12000.0, seed: int = 9, steps_at_half_hz: int = 1280, log=print) -> list:
+    """How far the solver's own traces are from the lateral symmetry that the structured surrogate
+    assumes, against grid resolution: for each Ricker peak frequency f0, `sources` random source
+    cells on the study's model, the 18 traces of `per_run` receivers (offset 1 km .. max_offset),
+    and the relative L2 residual of their best fit by 10 azimuth-independent fundamental traces
+    (`fundamentals`), overall and by offset.  The window grows as 1/f0 (steps_at_half_hz steps at
+    0.5 Hz), so every run sees the same arrivals.  Points per wavelength are given at f0 and at 2.5 f0 (the
+    Ricker spectrum's upper edge) for the slowest S velocity."""
+    out = []
+    for f0 in f0s:
+        nt = int(round(steps_at_half_hz * 0.5 / f0))
+        ds = make_dataset(train_runs=sources, test_runs=0, n=n, nt=nt, per_run=per_run, seed=seed,
+                          max_offset=max_offset, log=log, f0=f0, dx=dx)
+        if ds is None:
+            return []
+        m, Y, geo = ds["m"], ds["Y"], ds["geo"]
+        energy = np.linalg.norm(Y.astype(np.float64), axis=1)
+        live = energy > 1e-3 * np.median(energy)
+        R = mixing_matrices(geo[:, 2])
+        G = fundamentals(Y[live], R[live])
+        err = rel_l2(np.einsum("nof,nft->not", R[live], G), Y[live])
+        off = geo[live, 1]
+        vs_min = float(min(m.meta["vs"]))
+        bins = {}
+        for lo, hi in ((1000, 4000), (4000, 8000), (8000, 12000), (12000, 20000)):
+            sel = (off >= lo) & (off < hi)
+            if sel.any():
+                bins[f"{lo // 1000}-{hi // 1000} km"] = {"median": float(np.median(err[sel])), "n": int(sel.sum())}
+        out.append({"f0_hz": f0, "steps": nt, "dx_m": float(m.dx),
+                    "points_per_s_wavelength_at_f0": vs_min / f0 / m.dx,
+                    "points_per_s_wavelength_at_2.5f0": vs_min / (2.5 * f0) / m.dx,
+                    "gf_sets": int(live.sum()), "median": float(np.median(err)),
+                    "p90": float(np.percentile(err, 90)), "by_offset": bins})
+        log(f"f0 {f0}: floor median {out[-1]['median']:.4f}, p90 {out[-1]['p90']:.4f}")
+    return out
+
+
 def _dist():
     try:
         import torch.distributed as dist
@@ -583,12 +636,18 @@ def _dist():
 
 
 def study(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: int = 1280, per_run: int = 64,
-          steps: int = 6000, seed: int = 7, max_offset: float = 12000.0, log=print, **fit_kw) -> dict | None:
-    """The whole study; None on ranks other than 0 of a multi-GPU run."""
-    ds = make_dataset(train_runs, test_runs, n, nt, per_run, seed, max_offset, log)
+          steps: int = 6000, seed: int = 7, max_offset: float = 12000.0, log=print, decimate: int = 1,
+          forms=("structured",), **fit_kw) -> dict | None:
+    """The whole study (one dataset, one fit per network form: "structured", "harmonics" or
+    "full"); None on ranks other than 0 of a multi-GPU run."""
+    ds = make_dataset(train_runs, test_runs, n, nt, per_run, seed, max_offset, log, decimate=decimate)
     if ds is None:
         return None
-    return fit_and_evaluate(ds, steps=steps, seed=seed, log=log, **fit_kw)
+    res = {}
+    for form in forms:
+        kw = dict(fit_kw, structured=form == "structured", full=form == "full")
+        res[form] = fit_and_evaluate(ds, steps=steps, seed=seed, log=log, **kw)
+    return res[forms[0]] if len(forms) == 1 else res
 
 
 def gemm_benchmark(shapes=((4096, 12800, 512), (4096, 512, 512), (256, 12800, 512), (12800, 512, 256),
@@ -678,6 +737,9 @@ def main():
     ap.add_argument("--per-run", type=int, default=64)
     ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--max-offset", type=float, default=12000.0)
+    ap.add_argument("--decimate", type=int, default=1, help="keep every d-th time step of the traces")
+    ap.add_argument("--forms", default="structured", help="comma list of structured, harmonics, full")
+    ap.add_argument("--floor", action="store_true", help="only the symmetry-floor study against f0")
     ap.add_argument("--out", default="")
     a = ap.parse_args()
     import os
@@ -715,7 +777,11 @@ def main():
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    res = study(a.train_runs, a.test_runs, a.n, a.nt, per_run=a.per_run, steps=a.steps, max_offset=a.max_offset)
+    if a.floor:
+        res = symmetry_floor(n=a.n, per_run=a.per_run, max_offset=a.max_offset)
+    else:
+        res = study(a.train_runs, a.test_runs, a.n, a.nt, per_run=a.per_run, steps=a.steps, max_offset=a.max_offset,
+                    decimate=a.decimate, forms=tuple(a.forms.split(",")))
     if res is None:
         return
     print(json.dumps(res, indent=1))

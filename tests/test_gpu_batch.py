@@ -55,6 +55,34 @@ def test_batch_equals_solo_runs(cuda_device):
                 np.testing.assert_array_equal(b.seismograms(pid, r), ref.traces)
 
 
+def test_batch_tile_heights(cuda_device):
+    """Every CTA tile height gives the same bits (multi-RHS launches and the persistent family
+    launches alike); the autotuner picks one of them."""
+    probs = problems(nt=24)
+    ref = None
+    for ty in (4, 8, 16):
+        with Batch(probs) as b:
+            b.set_tile(ty)
+            assert b.tile() == ty
+            b.run(24)
+            got = [[b.seismograms(p, r) for r in range(len(rl))] + [b.field(p, 0, F.F_SXY)]
+                   for p, (_, rl) in enumerate(probs)]
+        if ref is None:
+            ref = got
+            m, rl = probs[0]
+            np.testing.assert_array_equal(got[0][2], solo(m, rl[2][0], rl[2][1], 24)[1])
+        else:
+            for a, c in zip(got, ref):
+                for x, y in zip(a, c):
+                    np.testing.assert_array_equal(x, y, err_msg=f"tile height {ty}")
+    with Batch(probs) as b:
+        b.autotune(3)
+        assert b.tile() in (4, 8, 16)
+        for bad in (2, 5, 32):
+            with pytest.raises(Exception):
+                b.set_tile(bad)
+
+
 def test_batch_graph_autotune_and_reset(cuda_device):
     probs = problems(nt=140)
     with Batch(probs) as b:

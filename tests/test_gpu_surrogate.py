@@ -247,3 +247,32 @@ def test_network_beats_nearest_neighbour(cuda_device):
     assert r["surrogate_rel_l2"]["median"] < 0.12, r["surrogate_rel_l2"]
     assert r["network_gain_median"] > 1.4, (r["surrogate_rel_l2"], r["nearest_neighbour_rel_l2"])
     assert r["gf_sets_per_s"]["surrogate_over_fdtd_all"] > 100
+
+
+def test_symmetry_floor_falls_with_resolution(cuda_device):
+    """The solver's departure from the lateral symmetry (the floor of the structured surrogate)
+    is a discretisation effect: halving the source's frequency (twice the points per wavelength)
+    lowers it by well over half, as a second-order scheme's direction-dependent errors do."""
+    from elanfmt_gb300 import surrogate as S
+
+    r = S.symmetry_floor(f0s=(0.5, 0.25), sources=6, n=96, per_run=32, max_offset=5000.0, steps_at_half_hz=640,
+                         log=lambda *a: None)
+    assert [x["f0_hz"] for x in r] == [0.5, 0.25] and all(x["gf_sets"] > 150 for x in r)
+    assert r[1]["points_per_s_wavelength_at_f0"] == pytest.approx(2 * r[0]["points_per_s_wavelength_at_f0"])
+    assert r[1]["median"] < 0.4 * r[0]["median"], r
+
+
+def test_five_input_network_and_fallback(cuda_device):
+    """The five-input form (source x, y, depth, receiver offset, azimuth -> 18 traces, no symmetry
+    assumed) trained on the same small study: it beats its nearest-neighbour method, and with the
+    solver as fallback no served GF set exceeds the 1e-3 bar."""
+    from elanfmt_gb300 import surrogate as S
+
+    r = S.study(train_runs=24, test_runs=8, n=96, nt=640, per_run=32, steps=1500, max_offset=5000.0,
+                forms=("structured", "full"), log=lambda *a: None)
+    f = r["full"]
+    assert f["features"].startswith("source x, y, depth")
+    assert f["surrogate_rel_l2"]["median"] < f["nearest_neighbour_rel_l2"]["median"], f
+    for form in ("structured", "full"):
+        assert r[form]["effective_max_rel_l2_served"] <= 1e-3
+        assert r[form]["gf_sets_per_s"]["with_fallback"] > 0
