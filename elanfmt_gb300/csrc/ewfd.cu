@@ -221,6 +221,7 @@ struct ewf_handle {
     SrcEntry *d_src = nullptr;
     int nsrc = 0;
     std::vector<SrcEntry> h_src;
+    StressSrc src_fuse{};   // two-kernel step: the sources the stress kernel applies (nsrc 0: k_inject does)
     long long *d_rec_off = nullptr;
     int *d_rec_comp = nullptr;
     int nrec = 0;
@@ -865,6 +866,28 @@ extern "C" int ewf_set_sources(ewf_handle *h, int32_t n, const int32_t *cijk, co
     h->nsrc = n;
     h->src_version++;
     h->graph_dirty = true;
+    // the stress kernel's threads apply the entries when all of them lie in its cells (k_inject
+    // covers the rest: cells on the staggered arrays' last planes, and grids too thin for BC1's
+    // plane-2 copy)
+    StressSrc f{};
+    bool fuse = n > 0 && h->p.nz >= 3;
+    f.i0 = f.j0 = INT32_MAX;
+    f.i1 = f.j1 = f.k1 = -1;
+    for (const SrcEntry &q : v) {
+        if (q.i >= h->p.nx || q.j >= h->p.ny || q.k >= h->p.nz) fuse = false;
+        f.i0 = std::min(f.i0, q.i);
+        f.i1 = std::max(f.i1, q.i);
+        f.j0 = std::min(f.j0, q.j);
+        f.j1 = std::max(f.j1, q.j);
+        f.k1 = std::max(f.k1, fused_src_plane(q.comp, q.k));
+    }
+    if (fuse) {
+        f.src = h->d_src;
+        f.nsrc = n;
+    } else {
+        f = StressSrc{};
+    }
+    h->src_fuse = f;
     return EWF_OK;
 }
 
@@ -971,10 +994,15 @@ static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t
 {
     const dim3 blk(TX, h->ty);
     const dim3 grd((h->p.nx + TX - 1) / TX, (h->p.ny + h->ty - 1) / h->ty, (h->p.nz + a.kchunk - 1) / a.kchunk);
+    StressSrc ss = h->src_fuse;
+    ss.stf = h->d_stf;
+    ss.nstf = (int)h->nstf;
+    ss.it_ptr = h->d_it;
+    ss.order = h->p.src_order;
     if (ev) cudaEventRecord(ev[0], h->stream);
-    k_stress<T, MODEL, DAMP><<<grd, blk, 0, h->stream>>>(a);
+    k_stress<T, MODEL, DAMP><<<grd, blk, 0, h->stream>>>(a, ss);
     if (ev) cudaEventRecord(ev[1], h->stream);
-    if (h->nsrc > 0)
+    if (h->nsrc > 0 && ss.nsrc == 0)
         k_inject<T><<<1, 32, 0, h->stream>>>(a, h->d_src, h->nsrc, h->d_stf, (int)h->nstf, h->d_it, h->p.src_order);
     if (ev) cudaEventRecord(ev[2], h->stream);
     k_velocity<T, MODEL, DAMP, KAHAN><<<grd, blk, 0, h->stream>>>(a);
@@ -1676,7 +1704,7 @@ extern "C" int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct)
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
 {
     if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *n = (h->fused || h->wave || h->sweep) ? 2 : 3 + (h->nsrc > 0 ? 1 : 0);
+    *n = (h->fused || h->wave || h->sweep) ? 2 : 3 + (h->nsrc > 0 && h->src_fuse.nsrc == 0 ? 1 : 0);
     return EWF_OK;
 }
 

@@ -11,8 +11,10 @@
 // only for cells whose value is never read back).
 //
 // One time step (reference order OK4:485-505 / ANISO:519-555):
-//   k_stress    stress update + damping, free surface BC1 fused at planes k = 0..2
-//   k_inject    moment-tensor point injection (before-BC1 semantics replayed exactly)
+//   k_stress    stress update + damping, free surface BC1 fused at planes k = 0..2, point sources
+//               applied by the threads that own their cells
+//   k_inject    point injection for sources outside the stress kernel's cells (before-BC1
+//               semantics replayed exactly), and for the other step forms
 //   k_velocity  velocity update + damping (optionally Kahan-compensated)
 //   k_record    receiver gather into FP64 traces; advances the device step counter
 // Expression order follows the reference so that an FMA-free build is bit-identical to the
@@ -62,6 +64,28 @@ struct SrcEntry {
     int comp, i, j, k;
     double coef;
 };
+
+// Point sources applied by the stress kernel itself (the two-kernel step): the thread that owns an
+// entry's column applies it right after its stores of the entry's plane -- for sxz / syz on plane
+// 1, after plane 2, whose update BC1 copies onto plane 1 -- with k_inject's arithmetic
+// (inject_entry), so the result is bit-identical to the separate launch.  [i0, i1] x [j0, j1]
+// bounds the entries' columns, so every other thread skips them with one test per plane.
+struct StressSrc {
+    const SrcEntry *src;  // nsrc entries, every one inside the stress kernel's cells (i < nx, j < ny, k < nz)
+    int nsrc;             // 0: none (k_inject applies the sources, if any)
+    const double *stf;
+    int nstf;
+    const int *it_ptr;
+    int order;            // 0: before BC1 (OK4), 1: after (ANISO)
+    int i0, i1, j0, j1;   // bounding box of the entries' columns
+    int k1;               // last effective plane of any entry
+};
+
+// The plane after whose stores the stress kernel applies an entry.
+__host__ __device__ __forceinline__ int fused_src_plane(int comp, int k) { return (k == 1 && (comp == 7 || comp == 8)) ? 2 : k; }
+
+template <typename T>
+__device__ __forceinline__ void inject_entry(const StepArgs<T> &a, const SrcEntry &q, T s, int order);
 
 template <typename T>
 __device__ __forceinline__ T ld(const T *p) { return __ldg(p); }
@@ -294,8 +318,9 @@ __device__ __forceinline__ void stress_store(const StepArgs<T> &a, long long c, 
 // RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
 // SOFF (with RC = 1): the state lives soff elements after the materials' index (one of several
 // right-hand sides in separate boxes of the same geometry).  COH: coherent state loads (lds).
-template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false, int COH = 0>
-__device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1, long long soff = 0)
+template <typename T, int MODEL, int DAMP, int RC, bool SOFF = false, int COH = 0, bool SRC = false>
+__device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j, int k0, int k1, long long soff = 0,
+                                              const StressSrc &ss = StressSrc{})
 {
     constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices
     const int R = RC ? RC : a.R;
@@ -315,6 +340,14 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
     if (DAMP == DAMP_PML1D) wz_k = ld(a.w1[2] + k0);
     StressIn<T, MODEL, DAMP> nxt;
     stress_load<T, MODEL, DAMP, RC, COH>(a, c, SEP ? cm : c, k0, nxt);
+    // point sources on this column (SRC: the two-kernel step's stress kernel)
+    bool src_col = false;
+    T s_src = T(0);
+    if (SRC && ss.nsrc > 0 && i >= ss.i0 && i <= ss.i1 && j >= ss.j0 && j <= ss.j1 && k0 <= ss.k1) {
+        const int it = *ss.it_ptr;
+        src_col = it >= 0 && it < ss.nstf;  // the host validates the step range; never read past Src
+        if (src_col) s_src = (T)ss.stf[it];
+    }
 
     for (int k = k0; k < k1; ++k, c += sys) {
         if (SEP && k > k0) cm += sy;
@@ -324,6 +357,12 @@ __device__ __forceinline__ void stress_column(const StepArgs<T> &a, int X, int j
         bool w_xy, w_xz, w_yz;
         stress_math<T, MODEL, DAMP>(a, q, cd, i, j, k, vx_m, vy_m, vz_k, wz_k, o, w_xy, w_xz, w_yz);
         stress_store<T>(a, c, sys, k, i, j, row_bc, o, w_xy, w_xz, w_yz);
+        if (SRC && src_col && k <= ss.k1) {
+            for (int e = 0; e < ss.nsrc; ++e) {
+                const SrcEntry q_e = ss.src[e];
+                if (q_e.i == i && q_e.j == j && fused_src_plane(q_e.comp, q_e.k) == k) inject_entry(a, q_e, s_src, ss.order);
+            }
+        }
         if (MODEL == MODEL_ISO && DAMP == DAMP_PML1D) wz_k = q.w;
         vx_m = q.vx;
         vy_m = q.vy;
@@ -341,11 +380,13 @@ template <typename T>
 constexpr int split_min_ctas() { return sizeof(T) == 4 ? 2 : 1; }
 
 template <typename T, int MODEL, int DAMP>
-__global__ void __launch_bounds__(split_max_threads<T>(), split_min_ctas<T>()) k_stress(const StepArgs<T> a)
+__global__ void __launch_bounds__(split_max_threads<T>(), split_min_ctas<T>()) k_stress(const StepArgs<T> a,
+                                                                                        const StressSrc ss)
 {
     const int k0 = blockIdx.z * a.kchunk;
-    stress_column<T, MODEL, DAMP, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, k0,
-                                  min(k0 + a.kchunk, a.nz));
+    stress_column<T, MODEL, DAMP, 1, false, 0, true>(a, blockIdx.x * TX + threadIdx.x,
+                                                     blockIdx.y * blockDim.y + threadIdx.y, k0,
+                                                     min(k0 + a.kchunk, a.nz), 0, ss);
 }
 
 // ---------------------------------------------------------------------------------------------

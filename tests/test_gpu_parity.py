@@ -298,6 +298,29 @@ def sweep_case():
     return m
 
 
+@pytest.mark.parametrize("order", [F.SRC_BEFORE_BC1, F.SRC_AFTER_BC1], ids=["before-bc1", "after-bc1"])
+def test_split_step_sources_in_the_stress_kernel(cuda_device, order):
+    """The two-kernel step applies point sources in the stress kernel's owning threads when every
+    entry lies in its cells (no k_inject launch), and falls back to k_inject otherwise; both give
+    the oracle's bits -- entries on planes 0-2 (BC1), on chunk borders, several on one cell, and on
+    cells the stress update leaves unchanged."""
+    m = sweep_case()
+    m.src_order = order
+    inside = [q for q in range(len(m.sources))
+              if m.sources[q][1] < m.nx and m.sources[q][2] < m.ny and m.sources[q][3] < m.nz]
+    assert len(inside) < len(m.sources)
+    for sel, launches in ((list(range(len(m.sources))), 4), (inside, 3)):
+        mm = sweep_case()
+        mm.src_order = order
+        mm.sources, mm.source_coef = m.sources[sel], m.source_coef[sel]
+        ref = O.run(mm, 24)
+        with Solver.from_model(mm, kchunk=4, graph_steps=6) as s:
+            assert s.launches_per_step() == launches
+            s.run(24)
+            got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+        assert_bitwise(got, ref, f"{len(sel)} entries")
+
+
 def test_sweep_layouts(cuda_device):
     """The sweep step over its settings (CTAs per multiprocessor, velocity lag) and the
     autotuner's pick: every layout gives the oracle's bits."""
