@@ -9,7 +9,11 @@
  *
  *   ewfd --nbx 12 --nby 12 --nbz 7 [--overx 0 ...] [--model iso|ortho|isohet|dcq] [--nt N] [--vdamp C]
  *        [--precision f32|kahan|f64] [--src i,j,k] [--stencil ok4|aniso] [--mts FILE]
+ *        [--free-surface bc1|none] [--surface-mu MU]
  *        [--receivers FILE] [--snap-every N] [--workdir DIR] [--quiet] [--no-checks]
+ *
+ * --free-surface none drops BC1 (the diff_BC schemes comment its launch out); --surface-mu MU
+ * gives the isotropic scheme's shear modulus MU on plane k = 1 (the diff_BC2_OK3 scheme: 1e-5).
  *
  * Exit status is 0 on success and 1 on any error (the reference returns 0 even after a CUDA
  * failure, OK4:96-99, 558).
@@ -88,6 +92,14 @@ int main(int argc, char **argv)
             continue;
         }
         if (!strcmp(k, "--vdamp") && v) { p.vdamp = atof(v); ++a; continue; }
+        if (!strcmp(k, "--surface-mu") && v) { p.surface_mu = atof(v); ++a; continue; }
+        if (!strcmp(k, "--free-surface") && v) {
+            if (!strcmp(v, "none")) p.free_surface = EWF_FS_NONE;
+            else if (!strcmp(v, "bc1")) p.free_surface = EWF_FS_BC1;
+            else return fail(EWF_ERR_ARG, "--free-surface bc1|none");
+            ++a;
+            continue;
+        }
         if (!strcmp(k, "--precision") && v) {
             p.precision = !strcmp(v, "f64") ? EWF_PREC_F64 : !strcmp(v, "kahan") ? EWF_PREC_F32_KAHAN : EWF_PREC_F32;
             ++a;

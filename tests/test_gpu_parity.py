@@ -500,6 +500,36 @@ def test_legacy_file_contract_other_schemes(cuda_device, tmp_path, flag, model, 
     np.testing.assert_array_equal(out["Rec_all"], ref.traces.astype(np.float32))
 
 
+def test_legacy_file_contract_without_free_surface(cuda_device, tmp_path):
+    """The diff_BC2_OK3 scheme through the executable: the isotropic file set with
+    `--free-surface none --surface-mu 1e-5` (no BC1, shear modulus 1e-5 on plane 1)."""
+    m = I.random_small(F.MODEL_ISO, 40, 44, 24, nt=40, seed=21)
+    m.free_surface = F.FS_NONE
+    m.surface_mu = 1e-5
+    xs, ys, zs = 12, 13, 1
+    m.set_moment_tensor(np.array([0.0, 0.0, 0.0, 0.0, 1.0, 0.8]), xs, ys, zs, 0)
+    m.receivers = np.array([[30, 20, 1, F.F_VZ], [30, 20, 1, F.F_VX], [30, 23, 1, F.F_VY], [30, 22, 1, F.F_VY]],
+                           np.int32)
+    L.write_inputs(m, str(tmp_path))
+    with open(tmp_path / "rec.txt", "w") as fh:
+        for r in m.receivers:
+            fh.write(" ".join(str(int(v)) for v in r) + "\n")
+    exe = os.path.join(ROOT, "elanfmt_gb300", "ewfd")
+    r = subprocess.run([exe, "--nx", "40", "--ny", "44", "--nz", "24", "--workdir", str(tmp_path), "--src",
+                        f"{xs},{ys},{zs}", "--receivers", str(tmp_path / "rec.txt"), "--free-surface", "none",
+                        "--surface-mu", "1e-5", "--quiet"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = L.read_outputs(str(tmp_path), m.nt)
+    ref = O.run(m, 40)
+    for q, name in ((F.F_VX, "Vx"), (F.F_VY, "Vy"), (F.F_VZ, "Vz")):
+        np.testing.assert_array_equal(out[name], ref.f[q])
+    for q, name in enumerate(("Rec", "Rec_x", "Rec_y", "Rec_y2")):
+        np.testing.assert_array_equal(out[name], ref.traces[q].astype(np.float32))
+    bad = subprocess.run([exe, "--nx", "40", "--ny", "44", "--nz", "24", "--workdir", str(tmp_path),
+                          "--free-surface", "sometimes", "--quiet"], capture_output=True, text=True)
+    assert bad.returncode == 1 and "--free-surface" in bad.stderr
+
+
 def test_async_snapshots_are_the_fields_at_their_step(cuda_device, tmp_path):
     """Queued snapshots (device copy in stream order, D2H on a second stream, files by a library
     thread) hold the fields of the step they were requested at, while later steps run; three
