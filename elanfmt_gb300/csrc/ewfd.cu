@@ -237,6 +237,7 @@ struct ewf_handle {
     float last_ms = 0.f;
     int kchunk = 32;
     int ty = TY;        // two-kernel step: CTA tile height in rows (autotuned)
+    bool pdl = true;    // two-kernel step: kernels launched as programmatic dependents (off if capture refuses)
     bool fdiv = false;  // div_spacing verified for (float) dx, dy, dz
     struct Snapshots *snap = nullptr;  // queued snapshot writer (created on first use)
 };
@@ -989,6 +990,24 @@ extern "C" int ewf_reset(ewf_handle *h)
 // ------------------------------------------------------------------------------------------
 // the time step
 // ------------------------------------------------------------------------------------------
+// A launch on the handle's stream; `pdl`: as a programmatic dependent of the stream's previous
+// kernel (the kernel waits for it with griddepcontrol.wait before touching any state).
+template <typename... P, typename... A>
+static void launch_on(void (*kern)(P...), dim3 grid, dim3 block, cudaStream_t stream, bool pdl, A... args)
+{
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <typename T, int MODEL, int DAMP, bool KAHAN>
 static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t *ev)
 {
@@ -999,15 +1018,18 @@ static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t
     ss.nstf = (int)h->nstf;
     ss.it_ptr = h->d_it;
     ss.order = h->p.src_order;
+    const bool pdl = h->pdl && !ev;  // kernels timed between events run as plain launches
     if (ev) cudaEventRecord(ev[0], h->stream);
-    k_stress<T, MODEL, DAMP><<<grd, blk, 0, h->stream>>>(a, ss);
+    launch_on(k_stress<T, MODEL, DAMP>, grd, blk, h->stream, pdl, a, ss);
     if (ev) cudaEventRecord(ev[1], h->stream);
     if (h->nsrc > 0 && ss.nsrc == 0)
-        k_inject<T><<<1, 32, 0, h->stream>>>(a, h->d_src, h->nsrc, h->d_stf, (int)h->nstf, h->d_it, h->p.src_order);
+        launch_on(k_inject<T>, dim3(1), dim3(32), h->stream, pdl, a, (const SrcEntry *)h->d_src, h->nsrc,
+                  (const double *)h->d_stf, (int)h->nstf, (const int *)h->d_it, h->p.src_order);
     if (ev) cudaEventRecord(ev[2], h->stream);
-    k_velocity<T, MODEL, DAMP, KAHAN><<<grd, blk, 0, h->stream>>>(a);
+    launch_on(k_velocity<T, MODEL, DAMP, KAHAN>, grd, blk, h->stream, pdl, a);
     if (ev) cudaEventRecord(ev[3], h->stream);
-    k_record<T><<<1, 256, 0, h->stream>>>(a, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    launch_on(k_record<T>, dim3(1), dim3(256), h->stream, pdl, a, (const long long *)h->d_rec_off,
+              (const int *)h->d_rec_comp, h->nrec, h->d_traces, (int)h->p.nt, h->d_it);
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
@@ -1433,6 +1455,11 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     bool graph = use_graph;
     if (graph && (h->graph_dirty || !h->gexec)) {
         st = build_graph(h, fn);
+        if (st && h->pdl && !h->sweep) {  // a driver that cannot capture dependent launches: plain ones
+            cudaGetLastError();
+            h->pdl = false;
+            st = build_graph(h, fn);
+        }
         if (st && h->sweep) {  // a driver that cannot capture the cooperative launch: launch directly
             cudaGetLastError();
             h->gsteps = 0;
@@ -1663,6 +1690,21 @@ extern "C" int ewf_set_tile(ewf_handle *h, int32_t tile_y)
         return ewf_fail(EWF_ERR_ARG, "tile_y must be a power of two in [1, %d] (got %d)", mx, tile_y);
     h->ty = tile_y;
     h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_dependent_launch(ewf_handle *h, int32_t on)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    h->pdl = on != 0;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_dependent_launch(const ewf_handle *h, int32_t *on)
+{
+    if (!h || !on) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *on = h->pdl ? 1 : 0;
     return EWF_OK;
 }
 

@@ -90,6 +90,15 @@ __device__ __forceinline__ void inject_entry(const StepArgs<T> &a, const SrcEntr
 template <typename T>
 __device__ __forceinline__ T ld(const T *p) { return __ldg(p); }
 
+// Programmatic dependent launch.  The two-kernel step launches each kernel as a programmatic
+// dependent of the previous one, so its CTAs are scheduled while the previous kernel's last wave
+// runs instead of after a full launch gap.  Each kernel lets its dependent launch at once
+// (pdl_trigger) and, before touching any state, waits until the previous grid has completed and
+// its stores are visible (pdl_wait) -- so no read and no write moves ahead of the dependency.
+// Launched without the attribute, both are no-ops.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // State loads.  COH = 0: the read-only path (the field is not written during the launch).
 // COH = 1: a plain coherent load, for the wavefront step, where other CTAs of the same launch
 // write the fields (ordered by its release/acquire flags).  COH = 2: a load cached in L2 only
@@ -383,6 +392,8 @@ template <typename T, int MODEL, int DAMP>
 __global__ void __launch_bounds__(split_max_threads<T>(), split_min_ctas<T>()) k_stress(const StepArgs<T> a,
                                                                                         const StressSrc ss)
 {
+    pdl_trigger();
+    pdl_wait();
     const int k0 = blockIdx.z * a.kchunk;
     stress_column<T, MODEL, DAMP, 1, false, 0, true>(a, blockIdx.x * TX + threadIdx.x,
                                                      blockIdx.y * blockDim.y + threadIdx.y, k0,
@@ -416,6 +427,8 @@ template <typename T>
 __global__ void k_inject(const StepArgs<T> a, const SrcEntry *__restrict__ src, int nsrc,
                          const double *__restrict__ stf, int nstf, const int *__restrict__ it_ptr, int order)
 {
+    pdl_trigger();
+    pdl_wait();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int it = *it_ptr;
     if (it < 0 || it >= nstf) return;  // the host validates the step range; never read past Src
@@ -617,6 +630,8 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
 template <typename T, int MODEL, int DAMP, bool KAHAN>
 __global__ void __launch_bounds__(split_max_threads<T>()) k_velocity(const StepArgs<T> a)
 {
+    pdl_trigger();
+    pdl_wait();
     const int k0 = blockIdx.z * a.kchunk;
     velocity_column<T, MODEL, DAMP, KAHAN, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y,
                                            k0, min(k0 + a.kchunk, a.nz));
@@ -630,6 +645,8 @@ template <typename T>
 __global__ void k_record(const StepArgs<T> a, const long long *__restrict__ rec_off, const int *__restrict__ rec_comp,
                          int nrec, double *__restrict__ traces, int trace_len, int *it_ptr)
 {
+    pdl_trigger();
+    pdl_wait();
     const int it = *it_ptr;
     if (it >= 0 && it < trace_len)
         for (int r = threadIdx.x; r < nrec; r += blockDim.x)

@@ -77,6 +77,8 @@ SIGNATURES = {
     "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_set_dependent_launch": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_get_dependent_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_wave_hold": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
@@ -298,6 +300,15 @@ class Solver:
         ty = C.c_int32()
         _check(self._lib.ewf_get_tile(self._h, C.byref(ty)), "ewf_get_tile")
         return ty.value
+
+    def set_dependent_launch(self, on: bool) -> None:
+        """Two-kernel step: programmatic dependent launches (default on; results do not depend on it)."""
+        _check(self._lib.ewf_set_dependent_launch(self._h, int(bool(on))), "ewf_set_dependent_launch")
+
+    def dependent_launch(self) -> bool:
+        v = C.c_int32()
+        _check(self._lib.ewf_get_dependent_launch(self._h, C.byref(v)), "ewf_get_dependent_launch")
+        return bool(v.value)
 
     def set_wave(self, lag_pct: int) -> None:
         """Wavefront step: lag of the velocity items behind the stress items, percent of the resident

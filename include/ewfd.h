@@ -224,6 +224,13 @@ int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
  * z-chunk; results do not depend on it.  ewf_set_tile: EWF_ERR_STATE for the other step forms. */
 int ewf_set_tile(ewf_handle *h, int32_t tile_y);
 int ewf_get_tile(const ewf_handle *h, int32_t *tile_y);
+/* Two-kernel step: launch each kernel as a programmatic dependent of the previous one (1, the
+ * default), so its CTAs are scheduled while the previous kernel finishes instead of after a launch
+ * gap; every kernel still waits for the previous grid before it touches the state.  0: plain
+ * stream-ordered launches.  The handle turns it off by itself if graph capture refuses it.
+ * Results do not depend on it. */
+int ewf_set_dependent_launch(ewf_handle *h, int32_t on);
+int ewf_get_dependent_launch(const ewf_handle *h, int32_t *on);
 
 /* Wavefront step (fused = EWF_STEP_WAVE): the lag of the velocity items behind the stress items
  * in percent of the resident CTAs, 1..100000 (set by ewf_autotune; results do not depend on it).

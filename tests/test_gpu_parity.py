@@ -298,6 +298,21 @@ def sweep_case():
     return m
 
 
+def test_split_step_dependent_launches(cuda_device):
+    """Programmatic dependent launches (default) and plain launches give the same bits, in the
+    captured graph and on the direct path (steps left over after the graph launches)."""
+    m = I.random_small(F.MODEL_ORTHO, 35, 37, 21, nt=30, seed=57, damping=F.DAMP_SEPARABLE)
+    ref = O.run(m, 30)
+    for on in (True, False):
+        with Solver.from_model(m, kchunk=6, graph_steps=8) as s:
+            assert s.dependent_launch()
+            s.set_dependent_launch(on)
+            s.run(30)
+            assert s.dependent_launch() == on
+            got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
+        assert_bitwise(got, ref, f"dependent launches {on}")
+
+
 @pytest.mark.parametrize("order", [F.SRC_BEFORE_BC1, F.SRC_AFTER_BC1], ids=["before-bc1", "after-bc1"])
 def test_split_step_sources_in_the_stress_kernel(cuda_device, order):
     """The two-kernel step applies point sources in the stress kernel's owning threads when every
