@@ -120,27 +120,17 @@ __device__ __forceinline__ void sweep_prefetch_plane(const SweepArgs<T> &sa, con
 }
 
 // named CTA barriers (ids 1-6; 0 is __syncthreads): arrive without waiting / arrive and wait.
-// The id is an immediate in each instruction: with an id in a register the assembler has to
-// reserve all sixteen barriers of the CTA, which limits how many CTAs an SM takes.
-template <int ID>
-__device__ __forceinline__ void bar_op(bool wait, int count)
+// bar.sync / bar.arrive are the warp-aligned forms: every thread of a warp must execute the same
+// instruction together, so each call site is one instruction and every caller reconverges its
+// warp (__syncwarp) right before it -- the code ahead of a barrier has per-thread branches.
+__device__ __forceinline__ void bar_arrive(int id, int count)
 {
-    if (wait) asm volatile("bar.sync %0, %1;" ::"n"(ID), "r"(count) : "memory");
-    else asm volatile("bar.arrive %0, %1;" ::"n"(ID), "r"(count) : "memory");
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
-__device__ __forceinline__ void bar_id(int id, bool wait, int count)
+__device__ __forceinline__ void bar_sync(int id, int count)
 {
-    switch (id) {
-        case 1: bar_op<1>(wait, count); break;
-        case 2: bar_op<2>(wait, count); break;
-        case 3: bar_op<3>(wait, count); break;
-        case 4: bar_op<4>(wait, count); break;
-        case 5: bar_op<5>(wait, count); break;
-        default: bar_op<6>(wait, count); break;
-    }
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
-__device__ __forceinline__ void bar_arrive(int id, int count) { bar_id(id, false, count); }
-__device__ __forceinline__ void bar_sync(int id, int count) { bar_id(id, true, count); }
 __device__ __forceinline__ int bar_stored(int p) { return 1 + (p & 1); }
 // grants run SWEEP_GRANT = 2 iterations ahead, so up to three "cleared" phases can be open at
 // once (four ids); "stored" has at most two open
@@ -241,6 +231,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? SWEEP_MAX_THREADS : SWEEP_MAX
         for (int p = 0; p < niter; ++p) {
             // while the compute warps work on plane p: input plane p + pfd into L2
             if (sa.pfd > 0 && p + sa.pfd <= nz) sweep_prefetch_plane(sa, me, p + sa.pfd, lane);
+            __syncwarp();
             bar_sync(bar_stored(p), nbar);  // every compute warp has stored its stresses of plane p
             if (p < nz && lane == 0) {
                 const int e0 = e;
@@ -330,6 +321,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? SWEEP_MAX_THREADS : SWEEP_MAX
             vy_m = q.vy;
             vz_k = q.vz_p;
         }
+        __syncwarp();
         bar_arrive(bar_stored(p), nbar);  // this warp's stores of plane p come first
         // velocity of plane kc from the inputs loaded last iteration
         const int kc = p - L - 1;
@@ -355,6 +347,7 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? SWEEP_MAX_THREADS : SWEEP_MAX
                 for (int f = 0; f < 3; ++f) vq.cp[f] = a.comp[f][cl];
             }
         }
+        __syncwarp();
         bar_sync(bar_cleared(p), nbar);  // neighbours and this CTA cover velocity plane kl
         if (vload) {
             if (kl == 1) {
