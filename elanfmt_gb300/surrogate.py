@@ -386,15 +386,17 @@ def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: i
     grid) for nt time steps and keeps, per source, `per_run` receivers with offsets in 1 km ..
     max_offset, every `decimate`-th sample.  Under torch.distributed the sources are shared out
     over the ranks (elanfmt_gb300.runs) and only rank 0 gets the dataset (None elsewhere)."""
-    m = layered_iso(n=n, nt=nt, f0=f0, dx=dx)
+    # geometry in metres (the cell counts below are those of dx = 120 m): a 1.8 km PML, receivers
+    # every 360 m, sources from 1.2 km inside the PML over 4 km
+    m = layered_iso(n=n, nt=nt, f0=f0, dx=dx, lpml=int(round(1800.0 / dx)))
     lpml = m.meta["lpml"]
-    rec_xy = surface_receivers(n, lpml, 3)
+    rec_xy = surface_receivers(n, lpml, max(1, int(round(360.0 / dx))))
     rng = np.random.default_rng(seed)
     nrun = train_runs + test_runs
     zlo = int(round(2000 / m.dz))
     zhi = min(int(round(8000 / m.dz)), n - lpml - 4)
-    span = max(4, min(int(4000 / m.dx), n - 2 * lpml - 20))
-    x0 = lpml + 10                                         # sources 10 cells inside the PML
+    x0 = lpml + int(round(1200.0 / dx))
+    span = max(4, min(int(4000 / m.dx), n - lpml - x0 - int(round(1200.0 / dx))))
     src = np.stack([rng.integers(x0, x0 + span, nrun), rng.integers(x0, x0 + span, nrun),
                     rng.integers(zlo, zhi + 1, nrun)], axis=1).astype(np.int32)
     geo = geometry(m, src, rec_xy)                         # [nrun, nrec, 4]
@@ -589,18 +591,21 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
     }
 
 
-def symmetry_floor(f0s=(0.5, 0.35, 0.25), sources: int = 16, n: int = 192, dx: float = 120.0, per_run: int = 64,
+def symmetry_floor(cases=((0.5, 120.0), (0.5, 60.0)), sources: int = 16, n120: int = 192, per_run: int = 64,
                    max_offset: float = 12000.0, seed: int = 9, steps_at_half_hz: int = 1280, log=print) -> list:
     """How far the solver's own traces are from the lateral symmetry that the structured surrogate
-    assumes, against grid resolution: for each Ricker peak frequency f0, `sources` random source
-    cells on the study's model, the 18 traces of `per_run` receivers (offset 1 km .. max_offset),
-    and the relative L2 residual of their best fit by 10 azimuth-independent fundamental traces
-    (`fundamentals`), overall and by offset.  The window grows as 1/f0 (steps_at_half_hz steps at
-    0.5 Hz), so every run sees the same arrivals.  Points per wavelength are given at f0 and at 2.5 f0 (the
-    Ricker spectrum's upper edge) for the slowest S velocity."""
+    assumes, against grid resolution: for each (Ricker peak frequency f0, cell size dx), the
+    same physical model (n120 cells of 120 m, so n120 * 120 / dx cells), `sources` random source
+    cells, the 18 traces of `per_run` receivers (offset 1 km .. max_offset), and the relative L2
+    residual of their best fit by 10 azimuth-independent fundamental traces (`fundamentals`),
+    overall and by offset.  The window is steps_at_half_hz steps of the 120 m grid at 0.5 Hz,
+    longer as 1/f0 and finer grids take more steps, so every case sees the same arrivals.  Points
+    per wavelength are given at f0 and at 2.5 f0 (the Ricker spectrum's upper edge) for the
+    slowest S velocity."""
     out = []
-    for f0 in f0s:
-        nt = int(round(steps_at_half_hz * 0.5 / f0))
+    for f0, dx in cases:
+        n = int(round(n120 * 120.0 / dx))
+        nt = int(round(steps_at_half_hz * (0.5 / f0) * (120.0 / dx)))
         ds = make_dataset(train_runs=sources, test_runs=0, n=n, nt=nt, per_run=per_run, seed=seed,
                           max_offset=max_offset, log=log, f0=f0, dx=dx)
         if ds is None:
@@ -618,12 +623,12 @@ def symmetry_floor(f0s=(0.5, 0.35, 0.25), sources: int = 16, n: int = 192, dx: f
             sel = (off >= lo) & (off < hi)
             if sel.any():
                 bins[f"{lo // 1000}-{hi // 1000} km"] = {"median": float(np.median(err[sel])), "n": int(sel.sum())}
-        out.append({"f0_hz": f0, "steps": nt, "dx_m": float(m.dx),
+        out.append({"f0_hz": f0, "dx_m": float(m.dx), "n": n, "steps": nt,
                     "points_per_s_wavelength_at_f0": vs_min / f0 / m.dx,
                     "points_per_s_wavelength_at_2.5f0": vs_min / (2.5 * f0) / m.dx,
                     "gf_sets": int(live.sum()), "median": float(np.median(err)),
                     "p90": float(np.percentile(err, 90)), "by_offset": bins})
-        log(f"f0 {f0}: floor median {out[-1]['median']:.4f}, p90 {out[-1]['p90']:.4f}")
+        log(f"f0 {f0} dx {dx}: floor median {out[-1]['median']:.4f}, p90 {out[-1]['p90']:.4f}")
     return out
 
 
@@ -778,7 +783,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     if a.floor:
-        res = symmetry_floor(n=a.n, per_run=a.per_run, max_offset=a.max_offset)
+        res = symmetry_floor(cases=((0.5, 120.0), (0.25, 120.0), (0.5, 60.0)), n120=a.n, per_run=a.per_run,
+                             max_offset=a.max_offset)
     else:
         res = study(a.train_runs, a.test_runs, a.n, a.nt, per_run=a.per_run, steps=a.steps, max_offset=a.max_offset,
                     decimate=a.decimate, forms=tuple(a.forms.split(",")))
