@@ -57,9 +57,8 @@ def parse():
     ap.add_argument("--size", type=str, default="", help="override grid, e.g. 128x128x96 (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e, cpu baseline, reference_gpu, kernel timing")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--step", default="split", choices=["split", "fused", "wave", "sweep"],
-                    help="step form: two kernels (default), the one-pass kernel, the wavefront launch or the "
-                         "lockstep sweep")
+    ap.add_argument("--step", default="split", choices=["split", "fused", "wave"],
+                    help="step form: two kernels (default), the one-pass kernel or the wavefront launch")
     ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
     ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
     return ap.parse_args()
@@ -370,7 +369,7 @@ def main():
     torch.cuda.set_device(local)
     m, desc = workload(args.workload, args.nt, args.size)
     nt = m.nt
-    form = {"split": F.STEP_SPLIT, "fused": F.STEP_FUSED, "wave": F.STEP_WAVE, "sweep": F.STEP_SWEEP}[args.step]
+    form = {"split": F.STEP_SPLIT, "fused": F.STEP_FUSED, "wave": F.STEP_WAVE}[args.step]
     s = Solver.from_model(m, fused=form, kchunk=args.kchunk)
     # the library's autotuner (z-chunk; the wavefront lag too) unless both are given
     kchunk = args.kchunk if args.kchunk and (form != F.STEP_WAVE or args.wave_lag) else s.autotune(30)
@@ -405,8 +404,6 @@ def main():
                    "kchunk_autotuned": kchunk, "step": args.step,
                    **({"tile_y_autotuned": s.tile()} if form == F.STEP_SPLIT else {}),
                    **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {}),
-                   **({"sweep_layout": dict(zip(("ctas_per_sm", "lag", "l2_prefetch", "ctas"), s.sweep_layout()))}
-                      if form == F.STEP_SWEEP else {}),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (working set ~%.1f GB)" % (m.cells * 4 * 21 / 1e9)},
         "gpu_launches": launches,
@@ -426,7 +423,7 @@ def main():
             names = {"stress": "k_stress", "velocity": "k_velocity"}
         else:  # one kernel does the whole step: its compulsory bytes are the one-pass step's
             kb = {"stress": STEP_BYTES[args.workload]}
-            names = {"stress": {F.STEP_WAVE: "k_wave", F.STEP_SWEEP: "k_sweep"}.get(form, "k_step")}
+            names = {"stress": "k_wave" if form == F.STEP_WAVE else "k_step"}
         kernels = {}
         for k in kb:
             achieved = kb[k] * m.cells / (kt[k] * 1e-3) / 1e9

@@ -10,7 +10,6 @@
 #include "ewfd_kernels.cuh"
 #include "ewfd_fused.cuh"
 #include "ewfd_wave.cuh"
-#include "ewfd_sweep.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -183,8 +182,7 @@ struct ewf_handle {
     void *f_alloc[9] = {};
     void *g_alloc[9] = {};  // second state buffer of the fused step
     bool fused = false;
-    bool sweep = false;     // lockstep sweep step (ewfd_sweep.cuh)
-    bool dbuf = false;      // double-buffered state (one-pass and sweep steps)
+    bool dbuf = false;      // double-buffered state (one-pass step)
     int flip = 0;           // double-buffered: the current state is in g_alloc when 1
     bool wave = false;      // wavefront step (ewfd_wave.cuh)
     int nsm = 0;            // multiprocessors of the device
@@ -198,17 +196,6 @@ struct ewf_handle {
     int src_version = 0;
     int wave_lag_pct = 100;     // lag = ntx + 1 + CTAs * pct / 100 (autotuned)
     int wave_hold = -1;         // diagnostic: stress item whose done flag is withheld
-    SweepCtl *d_sctl = nullptr;           // sweep step: generation, error flag, hold
-    unsigned long long *d_sflags = nullptr;  // progress flag per CTA
-    SweepCta *d_scta = nullptr;           // column range, neighbours and sources per CTA
-    SrcEntry *d_ssrc = nullptr;           // point sources grouped by CTA and plane
-    int sw_cap = 0, sw_src_cap = 0;       // capacities of d_sflags / d_scta and d_ssrc
-    int sw_per_sm = 2;                    // CTAs per multiprocessor (autotuned)
-    int sw_pfd = 4;                       // L2 prefetch distance in planes, 0 = off (autotuned)
-    int sw_lag = 4;                       // velocity plane = stress plane - lag - 1 (autotuned, >= 3)
-    int sw_ctas = 0, sw_nct = 0;          // the layout built: CTAs, compute threads per CTA
-    int sw_key[3] = {-1, -1, -1};         // (per_sm, src_version, hold) the layout was built for
-    int sw_hold = -1;                     // diagnostic: CTA whose progress is never published
     void *comp_alloc[3] = {};
     void *m_alloc[12] = {};
     bool m_set[12] = {};
@@ -473,10 +460,6 @@ extern "C" void ewf_destroy(ewf_handle *h)
     cudaFree(h->d_wdone);
     cudaFree(h->d_woff);
     cudaFree(h->d_wsrc);
-    cudaFree(h->d_sctl);
-    cudaFree(h->d_sflags);
-    cudaFree(h->d_scta);
-    cudaFree(h->d_ssrc);
     cudaFree(h->d_rec_off);
     cudaFree(h->d_rec_comp);
     cudaFree(h->d_traces);
@@ -500,7 +483,7 @@ static int validate_params(const ewf_params *p)
     if (p->precision < EWF_PREC_F32 || p->precision > EWF_PREC_F64) return ewf_fail(EWF_ERR_ARG, "unknown precision %d", p->precision);
     if (p->model == EWF_MODEL_ISO && p->damping != EWF_DAMP_PML1D && p->damping != EWF_DAMP_PERCOMP)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the isotropic scheme uses 1-D PML profiles or per-component weights (damping 0 or 3)");
-    if (p->fused < EWF_STEP_SPLIT || p->fused > EWF_STEP_SWEEP) return ewf_fail(EWF_ERR_ARG, "unknown step form %d", p->fused);
+    if (p->fused < EWF_STEP_SPLIT || p->fused > EWF_STEP_WAVE) return ewf_fail(EWF_ERR_ARG, "unknown step form %d", p->fused);
     if (p->damping == EWF_DAMP_PERCOMP && (p->model != EWF_MODEL_ISO || p->fused == EWF_STEP_FUSED))
         return ewf_fail(EWF_ERR_UNSUPPORTED, "per-component weights: isotropic model, two-kernel or wavefront step");
     if (p->model != EWF_MODEL_ISO && p->damping != EWF_DAMP_W3D && p->damping != EWF_DAMP_SEPARABLE)
@@ -557,7 +540,7 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
     h->kchunk = p->kchunk > 0 ? p->kchunk : 16;
     h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
-    if ((p->fused == EWF_STEP_FUSED || p->fused == EWF_STEP_SWEEP) && (h->gsteps & 1))
+    if (p->fused == EWF_STEP_FUSED && (h->gsteps & 1))
         h->gsteps += 1;  // double-buffered graphs replay buffer pairs
 
 #define CKH(call)                                                                                    \
@@ -581,8 +564,7 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     CKC(cudaEventCreate(&h->ev1));
     h->fused = p->fused == EWF_STEP_FUSED;
     h->wave = p->fused == EWF_STEP_WAVE;
-    h->sweep = p->fused == EWF_STEP_SWEEP;
-    h->dbuf = h->fused || h->sweep;
+    h->dbuf = h->fused;
     CKC(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
     if (h->wave) {
         CKC(cudaMalloc(&h->d_wctl, sizeof(WaveCtl)));
@@ -593,18 +575,6 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
     if (h->dbuf)
         for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->g_alloc[q]));
-    if (h->sweep) {
-        int coop = 0;
-        CKC(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->device));
-        if (!coop) {
-            ewf_destroy(h);
-            return ewf_fail(EWF_ERR_UNSUPPORTED, "the sweep step needs cooperative launches");
-        }
-        CKC(cudaMalloc(&h->d_sctl, sizeof(SweepCtl)));
-        CKC(cudaMemsetAsync(h->d_sctl, 0, sizeof(SweepCtl), h->stream));
-        const int nohold = -1;
-        CKC(cudaMemcpyAsync(&h->d_sctl->hold, &nohold, sizeof(int), cudaMemcpyHostToDevice, h->stream));
-    }
     if (p->precision == EWF_PREC_F32_KAHAN)
         for (int q = 0; q < 3; ++q) CKH(alloc_box(h, &h->comp_alloc[q]));
     for (int q = 0; q < n_materials(p->model); ++q)
@@ -1170,176 +1140,19 @@ static void wave_entry(const ewf_handle *h, cudaEvent_t *ev, int)
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
-// The sweep step: column ranges, neighbour ranges and the grouped point sources for the current
-// CTAs-per-multiprocessor setting, checked against the kernel's occupancy (every CTA must be
-// resident at once).  Rebuilt when the setting or the sources change; never during capture.
-static int sweep_prepare(ewf_handle *h, const void *kern)
-{
-    if (!h->sweep) return EWF_OK;
-    if (h->sw_ctas > 0 && h->sw_key[0] == h->sw_per_sm && h->sw_key[1] == h->src_version) return EWF_OK;
-    const int nx = h->p.nx, ny = h->p.ny, nz = h->p.nz;
-    const long long ncols = (long long)nx * ny;
-    const int maxthr = h->esz == 4 ? SWEEP_MAX_THREADS : SWEEP_MAX_THREADS / 2;
-    long long ctas = (long long)h->sw_per_sm * std::max(1, h->nsm);
-    ctas = std::min(ctas, std::max(1LL, (ncols + 31) / 32));  // at least a warp of columns per CTA
-    const long long len = (ncols + ctas - 1) / ctas;
-    const long long nct = (len + 31) / 32 * 32;
-    if (nct + 32 > maxthr)
-        return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: %lld columns over %lld CTAs need %lld threads per CTA (at most %d)",
-                        ncols, ctas, nct + 32, maxthr);
-    int occ = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, (int)nct + 32, 0));
-    if ((long long)occ * h->nsm < ctas)
-        return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: %lld CTAs of %lld threads cannot all be resident (%d per SM)", ctas,
-                        nct + 32, occ);
-    CK(cudaStreamSynchronize(h->stream));
-    const int nc = (int)ctas;
-    std::vector<long long> st((size_t)nc + 1);
-    for (int c = 0; c <= nc; ++c) st[(size_t)c] = (long long)c * ncols / nc;
-    auto owner = [&](long long q) { return (int)(std::upper_bound(st.begin(), st.begin() + nc, q) - st.begin()) - 1; };
-    std::vector<SweepCta> t((size_t)nc);
-    for (int c = 0; c < nc; ++c) {
-        SweepCta &x = t[(size_t)c];
-        x.s = (int)st[(size_t)c];
-        x.e = (int)st[(size_t)c + 1];
-        x.lo = owner(std::max(0LL, (long long)x.s - nx));
-        x.hi = owner(std::min(ncols - 1, (long long)x.e - 1 + nx));
-    }
-    // sources: owner of the entry's column (cells past the last row or column go to the owner of
-    // the nearest column: the velocity update never reads them), then by plane, stable
-    const size_t ns = h->h_src.size();
-    std::vector<int> own(ns), plane(ns), idx(ns);
-    for (size_t e = 0; e < ns; ++e) {
-        const SrcEntry &q = h->h_src[e];
-        own[e] = owner((long long)std::min(q.i, nx - 1) + (long long)std::min(q.j, ny - 1) * nx);
-        plane[e] = sweep_src_plane(q, nz);
-        idx[e] = (int)e;
-    }
-    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) {
-        return own[(size_t)x] != own[(size_t)y] ? own[(size_t)x] < own[(size_t)y] : plane[(size_t)x] < plane[(size_t)y];
-    });
-    std::vector<SrcEntry> grouped(ns);
-    for (int c = 0; c < nc; ++c) t[(size_t)c].src0 = t[(size_t)c].src1 = 0;
-    for (size_t r = 0; r < ns; ++r) grouped[r] = h->h_src[(size_t)idx[r]];
-    for (int c = 0, r = 0; c < nc; ++c) {
-        t[(size_t)c].src0 = r;
-        while (r < (int)ns && own[(size_t)idx[(size_t)r]] == c) ++r;
-        t[(size_t)c].src1 = r;
-    }
-    if (nc > h->sw_cap) {
-        cudaFree(h->d_sflags);
-        cudaFree(h->d_scta);
-        h->d_sflags = nullptr;
-        h->d_scta = nullptr;
-        h->sw_cap = 0;
-        CK(cudaMalloc(&h->d_sflags, (size_t)nc * sizeof(unsigned long long)));
-        CK(cudaMemset(h->d_sflags, 0, (size_t)nc * sizeof(unsigned long long)));  // below every target
-        CK(cudaMalloc(&h->d_scta, (size_t)nc * sizeof(SweepCta)));
-        h->sw_cap = nc;
-    }
-    if ((int)ns > h->sw_src_cap) {
-        cudaFree(h->d_ssrc);
-        h->d_ssrc = nullptr;
-        h->sw_src_cap = 0;
-        CK(cudaMalloc(&h->d_ssrc, ns * sizeof(SrcEntry)));
-        h->sw_src_cap = (int)ns;
-    }
-    CK(cudaMemcpy(h->d_scta, t.data(), (size_t)nc * sizeof(SweepCta), cudaMemcpyHostToDevice));
-    if (ns) CK(cudaMemcpy(h->d_ssrc, grouped.data(), ns * sizeof(SrcEntry), cudaMemcpyHostToDevice));
-    h->sw_ctas = nc;
-    h->sw_nct = (int)nct;
-    h->sw_key[0] = h->sw_per_sm;
-    h->sw_key[1] = h->src_version;
-    h->graph_dirty = true;
-    return EWF_OK;
-}
-
-// reads and clears the sweep step's error flag (after the stream has been synchronised)
-static int sweep_check(ewf_handle *h)
-{
-    if (!h->sweep) return EWF_OK;
-    int err = 0;
-    CK(cudaMemcpy(&err, &h->d_sctl->err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) {
-        CK(cudaMemset(&h->d_sctl->err, 0, sizeof(int)));
-        return ewf_fail(EWF_ERR_CUDA, "sweep step: a wait for a neighbouring CTA gave up; the state of this run is invalid");
-    }
-    return EWF_OK;
-}
-
-template <typename T, int MODEL, int DAMP, bool KAHAN>
-static void sweep_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
-{
-    SweepArgs<T> sa;
-    memset(&sa, 0, sizeof(sa));
-    sa.a = make_args<T>(h, parity);
-    const StepArgs<T> out = make_args<T>(h, 1 - parity);
-    for (int q = 0; q < 9; ++q) sa.o[q] = out.f[q];
-    sa.cta = h->d_scta;
-    sa.src = h->d_ssrc;
-    sa.stf = h->d_stf;
-    sa.nstf = (int)h->nstf;
-    sa.it_ptr = h->d_it;
-    sa.order = h->p.src_order;
-    sa.flags = h->d_sflags;
-    sa.ctl = h->d_sctl;
-    sa.lag = h->sw_lag;
-    sa.nct = h->sw_nct;
-    // the arrays the control warp prefetches into L2: step n's state, materials, 3-D weights,
-    // the compensation of the compensated form
-    sa.pfd = h->sw_pfd;
-    sa.esz = (int)sizeof(T);
-    auto add_pf = [&](const void *p) {
-        if (p && sa.npf < SWEEP_MAX_PF) sa.pf[sa.npf++] = (const char *)p;
-    };
-    for (int q = 0; q < 9; ++q) add_pf(sa.a.f[q]);
-    for (int q = 0; q < 12; ++q) add_pf(sa.a.m[q]);
-    add_pf(sa.a.w3);
-    for (int q = 0; q < 6; ++q) add_pf(sa.a.w6[q]);
-    if (KAHAN)
-        for (int q = 0; q < 3; ++q) add_pf(sa.a.comp[q]);
-    cudaLaunchConfig_t cfg;
-    memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3((unsigned)h->sw_ctas);
-    cfg.blockDim = dim3((unsigned)h->sw_nct + 32);
-    cfg.stream = h->stream;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;  // every CTA resident at once (they wait on each other)
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    if (ev) cudaEventRecord(ev[0], h->stream);
-    cudaLaunchKernelEx(&cfg, k_sweep<T, MODEL, DAMP, KAHAN>, sa);
-    if (ev) {
-        cudaEventRecord(ev[1], h->stream);
-        cudaEventRecord(ev[2], h->stream);
-        cudaEventRecord(ev[3], h->stream);
-    }
-    k_record<T><<<1, 256, 0, h->stream>>>(out, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
-    if (ev) cudaEventRecord(ev[4], h->stream);
-}
-
-// A step form: the host function that launches one step, and (sweep) the kernel whose
-// occupancy bounds the launch.
-struct StepImpl {
-    step_fn fn;
-    const void *kern;
-};
-
+// A step form: the host function that launches one step.
 template <int FORM, typename T, int MODEL, int DAMP, bool KAHAN>
-static StepImpl entry()
+static step_fn entry()
 {
-    if constexpr (FORM == EWF_STEP_FUSED) return {fused_entry<T, MODEL, DAMP, KAHAN>, nullptr};
-    else if constexpr (FORM == EWF_STEP_WAVE) return {wave_entry<T, MODEL, DAMP, KAHAN>, nullptr};
-    else if constexpr (FORM == EWF_STEP_SWEEP)
-        return {sweep_entry<T, MODEL, DAMP, KAHAN>, (const void *)k_sweep<T, MODEL, DAMP, KAHAN>};
-    else return {step_entry<T, MODEL, DAMP, KAHAN>, nullptr};
+    if constexpr (FORM == EWF_STEP_FUSED) return &fused_entry<T, MODEL, DAMP, KAHAN>;
+    else if constexpr (FORM == EWF_STEP_WAVE) return &wave_entry<T, MODEL, DAMP, KAHAN>;
+    else return &step_entry<T, MODEL, DAMP, KAHAN>;
 }
 
 // FORM: EWF_STEP_*; the one-pass form exists for models 0 and 1 with 1-D, 3-D or separable
 // damping (validated), the others for every combination
 template <int FORM>
-static StepImpl pick_step_t(const ewf_params &p)
+static step_fn pick_step_t(const ewf_params &p)
 {
     constexpr int F2 = FORM == EWF_STEP_FUSED ? EWF_STEP_SPLIT : FORM;  // forms built for every model
     const bool iso = p.model == EWF_MODEL_ISO;
@@ -1374,27 +1187,21 @@ static StepImpl pick_step_t(const ewf_params &p)
     }
 }
 
-static StepImpl pick_impl(const ewf_handle *h)
+static step_fn pick_step(const ewf_handle *h)
 {
     if (h->fused) return pick_step_t<EWF_STEP_FUSED>(h->p);
     if (h->wave) return pick_step_t<EWF_STEP_WAVE>(h->p);
-    if (h->sweep) return pick_step_t<EWF_STEP_SWEEP>(h->p);
     return pick_step_t<EWF_STEP_SPLIT>(h->p);
 }
-static step_fn pick_step(const ewf_handle *h) { return pick_impl(h).fn; }
 
 // everything a step form needs built before its first launch (never during capture)
 static int step_prepare(ewf_handle *h)
 {
-    int st = wave_prepare(h);
-    if (!st) st = sweep_prepare(h, pick_impl(h).kern);
-    return st;
+    return wave_prepare(h);
 }
 static int step_check(ewf_handle *h)
 {
-    int st = wave_check(h);
-    if (!st) st = sweep_check(h);
-    return st;
+    return wave_check(h);
 }
 
 static int inputs_ready(const ewf_handle *h)
@@ -1455,18 +1262,12 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     bool graph = use_graph;
     if (graph && (h->graph_dirty || !h->gexec)) {
         st = build_graph(h, fn);
-        if (st && h->pdl && !h->sweep) {  // a driver that cannot capture dependent launches: plain ones
+        if (st && h->pdl) {  // a driver that cannot capture dependent launches: plain ones
             cudaGetLastError();
             h->pdl = false;
             st = build_graph(h, fn);
         }
-        if (st && h->sweep) {  // a driver that cannot capture the cooperative launch: launch directly
-            cudaGetLastError();
-            h->gsteps = 0;
-            graph = false;
-        } else if (st) {
-            return st;
-        }
+        if (st) return st;
     }
     CK(cudaEventRecord(h->ev0, h->stream));
     int done = 0;
@@ -1543,7 +1344,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
 }
 
 // Device time of `steps` steps from a reset state (one untimed step first); -1 when the current
-// settings cannot run (e.g. a sweep layout whose CTAs cannot all be resident).
+// settings cannot run.
 static int time_setting(ewf_handle *h, int steps, float *ms)
 {
     int st = ewf_reset(h);
@@ -1577,35 +1378,6 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     if (steps < 1) return ewf_fail(EWF_ERR_ARG, "nt too small to tune");
     if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
     float best = 1e30f;
-    if (h->sweep) {
-        // sweep step: CTAs per multiprocessor x the velocity lag x the L2 prefetch distance
-        int best_m = -1, best_l = h->sw_lag, best_pf = h->sw_pfd;
-        static const int pfd_cand[] = {0, 2, 4, 6};
-        for (int m = 1; m <= 4; ++m)
-            for (int lag = 3; lag <= 5; ++lag)
-                for (int pf : pfd_cand) {
-                    h->sw_per_sm = m;
-                    h->sw_lag = lag;
-                    h->sw_pfd = pf;
-                    h->graph_dirty = true;
-                    float ms = 0.f;
-                    if ((st = time_setting(h, steps, &ms))) return st;
-                    if (ms >= 0.f && ms < best) {
-                        best = ms;
-                        best_m = m;
-                        best_l = lag;
-                        best_pf = pf;
-                    }
-                }
-        if (best_m < 0) return ewf_fail(EWF_ERR_UNSUPPORTED, "sweep step: no layout fits this grid");
-        h->sw_per_sm = best_m;
-        h->sw_lag = best_l;
-        h->sw_pfd = best_pf;
-        h->graph_dirty = true;
-        if ((st = step_prepare(h))) return st;
-        if (kchunk) *kchunk = h->kchunk;
-        return ewf_reset(h);
-    }
     int best_k = h->kchunk, best_lag = h->wave_lag_pct, best_ty = h->ty;
     // wavefront step: slabs of 4..16 planes x lag (100000: every stress item before the first velocity item)
     static const int lag_pct[] = {50, 100, 200, 100000};
@@ -1645,46 +1417,10 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     return ewf_reset(h);
 }
 
-extern "C" int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag, int32_t prefetch)
-{
-    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
-    if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
-    if (ctas_per_sm < 1 || ctas_per_sm > 8) return ewf_fail(EWF_ERR_ARG, "ctas_per_sm must be in [1, 8] (got %d)", ctas_per_sm);
-    if (lag < SWEEP_GRANT + 1 || lag > 16)
-        return ewf_fail(EWF_ERR_ARG, "lag must be in [%d, 16] (got %d)", SWEEP_GRANT + 1, lag);
-    if (prefetch < 0 || prefetch > 32) return ewf_fail(EWF_ERR_ARG, "prefetch must be in [0, 32] (got %d)", prefetch);
-    h->sw_per_sm = ctas_per_sm;
-    h->sw_lag = lag;
-    h->sw_pfd = prefetch;
-    h->graph_dirty = true;
-    return EWF_OK;
-}
-
-extern "C" int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *prefetch, int32_t *ctas)
-{
-    if (!h || !ctas_per_sm || !lag || !prefetch || !ctas) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
-    *ctas_per_sm = h->sw_per_sm;
-    *lag = h->sw_lag;
-    *prefetch = h->sw_pfd;
-    *ctas = h->sw_ctas;
-    return EWF_OK;
-}
-
-extern "C" int ewf_sweep_hold(ewf_handle *h, int32_t cta)
-{
-    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
-    if (!h->sweep) return ewf_fail(EWF_ERR_STATE, "not a sweep-step handle");
-    if (cta < -1) return ewf_fail(EWF_ERR_ARG, "cta must be >= -1");
-    CK(cudaStreamSynchronize(h->stream));
-    CK(cudaMemcpy(&h->d_sctl->hold, &cta, sizeof(int), cudaMemcpyHostToDevice));
-    return EWF_OK;
-}
-
 extern "C" int ewf_set_tile(ewf_handle *h, int32_t tile_y)
 {
     if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
-    if (h->wave || h->fused || h->sweep) return ewf_fail(EWF_ERR_STATE, "the tile height applies to the two-kernel step");
+    if (h->wave || h->fused) return ewf_fail(EWF_ERR_STATE, "the tile height applies to the two-kernel step");
     const int mx = h->esz == 4 ? SPLIT_MAX_TY : TY;
     if (tile_y < 1 || tile_y > mx || (tile_y & (tile_y - 1)))
         return ewf_fail(EWF_ERR_ARG, "tile_y must be a power of two in [1, %d] (got %d)", mx, tile_y);
@@ -1746,7 +1482,7 @@ extern "C" int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct)
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
 {
     if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *n = (h->fused || h->wave || h->sweep) ? 2 : 3 + (h->nsrc > 0 && h->src_fuse.nsrc == 0 ? 1 : 0);
+    *n = (h->fused || h->wave) ? 2 : 3 + (h->nsrc > 0 && h->src_fuse.nsrc == 0 ? 1 : 0);
     return EWF_OK;
 }
 

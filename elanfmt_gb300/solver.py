@@ -81,10 +81,6 @@ SIGNATURES = {
     "ewf_get_dependent_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_wave_hold": (C.c_int, [C.c_void_p, C.c_int32]),
-    "ewf_set_sweep": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
-    "ewf_get_sweep": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
-                                C.POINTER(C.c_int32)]),
-    "ewf_sweep_hold": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_batch_create": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "ewf_batch_destroy": (None, [C.c_void_p]),
     "ewf_batch_set_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t, C.c_int32]),
@@ -173,7 +169,7 @@ class Solver:
     def from_model(cls, m, precision: int = F.PREC_F32, kchunk: int = 0, graph_steps: int = 0,
                    check_finite: bool = True, damping: int | None = None, nout: int = 0,
                    fused: int | None = None, workdir: str | None = None) -> "Solver":
-        """`fused`: the step form, F.STEP_SPLIT (default), F.STEP_FUSED, F.STEP_WAVE or F.STEP_SWEEP."""
+        """`fused`: the step form, F.STEP_SPLIT (default), F.STEP_FUSED or F.STEP_WAVE."""
         p = default_params()
         p.nx, p.ny, p.nz, p.nt = m.nx, m.ny, m.nz, m.nt
         p.model, p.precision = m.model, precision
@@ -323,20 +319,6 @@ class Solver:
         lag = C.c_int32()
         _check(self._lib.ewf_get_wave(self._h, C.byref(lag)), "ewf_get_wave")
         return lag.value
-
-    def set_sweep(self, ctas_per_sm: int, lag: int, prefetch: int = 4) -> None:
-        """Sweep step: CTAs per multiprocessor, velocity lag and L2 prefetch distance in planes
-        (results do not depend on them)."""
-        _check(self._lib.ewf_set_sweep(self._h, int(ctas_per_sm), int(lag), int(prefetch)), "ewf_set_sweep")
-
-    def sweep_layout(self) -> tuple[int, int, int, int]:
-        """Sweep step: (CTAs per multiprocessor, lag, prefetch distance, CTAs of the layout last built)."""
-        m, lag, pf, n = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
-        _check(self._lib.ewf_get_sweep(self._h, C.byref(m), C.byref(lag), C.byref(pf), C.byref(n)), "ewf_get_sweep")
-        return m.value, lag.value, pf.value, n.value
-
-    def sweep_hold(self, cta: int) -> None:
-        _check(self._lib.ewf_sweep_hold(self._h, int(cta)), "ewf_sweep_hold")
 
     def launches_per_step(self) -> int:
         n = C.c_int32()

@@ -71,14 +71,9 @@ typedef enum ewf_damping {
 typedef enum ewf_step_form {
     EWF_STEP_SPLIT = 0, /* stress kernel, injection, velocity kernel (reference order OK4:485-498) */
     EWF_STEP_FUSED = 1, /* one-pass step kernel, double-buffered state (models 0 and 1) */
-    EWF_STEP_WAVE = 2,  /* one persistent launch of the stress and velocity updates over tile x slab
+    EWF_STEP_WAVE = 2   /* one persistent launch of the stress and velocity updates over tile x slab
                          * items in dependency order, in place: the velocity update reads the new
                          * stresses back from L2 (every model, damping and precision) */
-    EWF_STEP_SWEEP = 3  /* one cooperative launch per step: every CTA resident, each owning a balanced
-                         * range of (i,j) columns, all sweeping z in lockstep -- stress of plane p,
-                         * then velocity of plane p - lag from the neighbours' new stresses in L2;
-                         * double-buffered state, one DRAM pass per step (every model, damping and
-                         * precision; grids up to about 2 x 152 x 736 columns nx*ny in FP32) */
 } ewf_step_form;
 
 typedef enum ewf_free_surface {
@@ -129,8 +124,7 @@ typedef struct ewf_params {
     int32_t kchunk;       /* planes per CTA of the z-marching kernels; 0 = autotuned/default */
     int32_t graph_steps;  /* steps captured per CUDA graph; 0 = default, <0 = no graph */
     int32_t check_finite; /* 1: ewf_run checks the receiver traces for NaN/Inf */
-    int32_t fused;        /* ewf_step_form: 0 (default) two kernels; 1 one-pass kernel; 2 wavefront;
-                           * 3 lockstep sweep */
+    int32_t fused;        /* ewf_step_form: 0 (default) two kernels; 1 one-pass kernel; 2 wavefront */
     double dx, dy, dz, dt; /* pa1[0..3] (OK4:404) */
     double c66;            /* isotropic shear modulus pa2[7] (OK4:405); PERCOMP: the xy one */
     double c44, c55;       /* PERCOMP shear moduli of yz and xz, pa2[5], pa2[6] */
@@ -215,8 +209,7 @@ int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
 /* Autotuner: times `nsteps` steps for each z-chunk candidate (planes per CTA) with CUDA events,
  * keeps the fastest (returned in *kchunk, may be NULL) and resets the state.  The two-kernel step
  * also tunes its tile height (4, 8, 16 rows; ewf_get_tile), the wavefront step its lag (both kept
- * in the handle); the sweep step tunes its CTAs per multiprocessor, lag and prefetch distance
- * instead of the z-chunk. */
+ * in the handle). */
 int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
 
 /* Two-kernel step (fused = EWF_STEP_SPLIT): the height of a CTA's tile in rows of 32 columns
@@ -242,19 +235,6 @@ int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct);
  * wait and ewf_run returns EWF_ERR_CUDA (the state of that run is invalid; the handle stays
  * usable after ewf_reset).  -1 restores normal operation. */
 int ewf_wave_hold(ewf_handle *h, int32_t item);
-
-/* Sweep step (fused = EWF_STEP_SWEEP): CTAs per multiprocessor (1..8; all CTAs must fit at once),
- * the lag of the velocity plane behind the stress plane (3..16) and how many planes ahead the
- * control warp prefetches the inputs into L2 (0..32, 0 = off), all set by ewf_autotune; results do
- * not depend on them.  ewf_get_sweep also returns the CTAs of the layout last built (0 before the
- * first run).  EWF_ERR_STATE for the other step forms. */
-int ewf_set_sweep(ewf_handle *h, int32_t ctas_per_sm, int32_t lag, int32_t prefetch);
-int ewf_get_sweep(const ewf_handle *h, int32_t *ctas_per_sm, int32_t *lag, int32_t *prefetch, int32_t *ctas);
-/* Diagnostic for tests of the failure path: CTA `cta` of the sweep step never publishes its
- * progress, so its neighbours give up after their bounded wait and ewf_run returns EWF_ERR_CUDA
- * (the state of that run is invalid; the handle stays usable after ewf_reset).  -1 restores
- * normal operation. */
-int ewf_sweep_hold(ewf_handle *h, int32_t cta);
 
 /* Writes 0_infos.inf and 0_0_{Src,Rec,Rec_x,Rec_y,Rec_y2,Vx,Vy,Vz}.res into workdir
  * (OK4:521-532).  Rec* are the first four receivers. */

@@ -49,10 +49,9 @@ CASES = [
 ]
 
 
-FUSED = pytest.mark.parametrize("fused", [F.STEP_FUSED, F.STEP_SPLIT, F.STEP_WAVE, F.STEP_SWEEP],
-                                ids=["fused", "split", "wave", "sweep"])
+FUSED = pytest.mark.parametrize("fused", [F.STEP_FUSED, F.STEP_SPLIT, F.STEP_WAVE], ids=["fused", "split", "wave"])
 # step forms built for every model and damping
-FORMS = pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_WAVE, F.STEP_SWEEP], ids=["split", "wave", "sweep"])
+FORMS = pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_WAVE], ids=["split", "wave"])
 
 
 @pytest.mark.parametrize("name,model,damping,nx,ny,nz", CASES, ids=[c[0] for c in CASES])
@@ -281,8 +280,8 @@ def test_split_tile_heights(cuda_device, prec):
     assert e.value.status == -5
 
 
-def sweep_case():
-    """A grid of a few hundred sweep CTAs with point sources on CTA-range borders, on several
+def border_source_case():
+    """A grid of a few hundred CTAs with point sources on tile and chunk borders, on several
     entries of one cell, and on cells the stress pass never updates (sxy at i = nx and at i = 0,
     sxz and syz on plane nz): their values are carried over from the previous step."""
     m = I.random_small(F.MODEL_ORTHO, 100, 72, 40, nt=24, seed=29, damping=F.DAMP_W3D, src_order=F.SRC_BEFORE_BC1)
@@ -319,13 +318,13 @@ def test_split_step_sources_in_the_stress_kernel(cuda_device, order):
     entry lies in its cells (no k_inject launch), and falls back to k_inject otherwise; both give
     the oracle's bits -- entries on planes 0-2 (BC1), on chunk borders, several on one cell, and on
     cells the stress update leaves unchanged."""
-    m = sweep_case()
+    m = border_source_case()
     m.src_order = order
     inside = [q for q in range(len(m.sources))
               if m.sources[q][1] < m.nx and m.sources[q][2] < m.ny and m.sources[q][3] < m.nz]
     assert len(inside) < len(m.sources)
     for sel, launches in ((list(range(len(m.sources))), 4), (inside, 3)):
-        mm = sweep_case()
+        mm = border_source_case()
         mm.src_order = order
         mm.sources, mm.source_coef = m.sources[sel], m.source_coef[sel]
         ref = O.run(mm, 24)
@@ -336,48 +335,7 @@ def test_split_step_sources_in_the_stress_kernel(cuda_device, order):
         assert_bitwise(got, ref, f"{len(sel)} entries")
 
 
-def test_sweep_layouts(cuda_device):
-    """The sweep step over its settings (CTAs per multiprocessor, velocity lag) and the
-    autotuner's pick: every layout gives the oracle's bits."""
-    m = sweep_case()
-    ref = O.run(m, 24)
-    for per_sm, lag, pf in ((1, 3, 0), (2, 4, 2), (3, 5, 4), (4, 3, 6), (2, 16, 32)):
-        with Solver.from_model(m, fused=F.STEP_SWEEP, graph_steps=6) as s:
-            s.set_sweep(per_sm, lag, pf)
-            s.run(24)
-            assert s.sweep_layout()[:3] == (per_sm, lag, pf)
-            assert s.sweep_layout()[3] > 32
-            got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
-        assert_bitwise(got, ref, f"ctas/SM {per_sm} lag {lag}")
-    with Solver.from_model(m, fused=F.STEP_SWEEP) as s:
-        s.autotune(4)
-        s.run(24)
-        got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
-    assert_bitwise(got, ref, "autotuned")
-    with Solver.from_model(m) as s, pytest.raises(EwfError) as e:
-        s.set_sweep(2, 3)
-    assert e.value.status == -5
-
-
-def test_sweep_wait_gives_up_and_handle_recovers(cuda_device):
-    """A CTA whose progress is never published (withheld by the diagnostic hook): its neighbours
-    give up after their bounded wait, ewf_run reports the failure instead of hanging, and after
-    a reset the same handle runs bit-exact again."""
-    m = I.random_small(F.MODEL_ORTHO, 64, 48, 24, nt=12, seed=31, damping=F.DAMP_W3D)
-    ref = O.run(m, 12)
-    with Solver.from_model(m, fused=F.STEP_SWEEP, graph_steps=-1) as s:
-        s.sweep_hold(7)
-        with pytest.raises(EwfError) as e:
-            s.run(2)
-        assert e.value.status == -2 and "gave up" in str(e.value)
-        s.sweep_hold(-1)
-        s.reset()
-        s.run(12)
-        got = ([s.field(q, np.float32) for q in F.STATE], s.seismograms())
-    assert_bitwise(got, ref, "after recovery")
-
-
-@pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_SWEEP], ids=["split", "sweep"])
+@pytest.mark.parametrize("form", [F.STEP_SPLIT, F.STEP_WAVE], ids=["split", "wave"])
 def test_workload_shapes_small(cuda_device, form):
     """The two benchmark workloads at reduced size, FP32, bit-exact."""
     m = I.iso_homogeneous(n=48, nt=120)
