@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define EWF_ABI_VERSION 4
+#define EWF_ABI_VERSION 5
 
 typedef enum ewf_status {
     EWF_OK = 0,
