@@ -256,6 +256,7 @@ def extra_iso(form: int) -> dict:
     """Isotropic homogeneous 128^3, 1000 steps, 8-receiver ring (the plain isotropic workload):
     Gcell-updates/s over full runs with the autotuned setting, the step roofline, and full-run
     seismogram parity against the reference's stock build."""
+    from elanfmt_gb300 import fields as F
     from elanfmt_gb300.solver import Solver
 
     m, desc = workload("iso", 0, "")
