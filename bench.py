@@ -61,6 +61,8 @@ def parse():
                     help="step form: two kernels (default), the one-pass kernel or the wavefront launch")
     ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
     ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
+    ap.add_argument("--batch-iso", type=int, default=16, help="batch workload: isotropic models beside the 6 MTs")
+    ap.add_argument("--no-reference", action="store_true", help="batch workload: skip the reference kernels' runs")
     return ap.parse_args()
 
 
@@ -280,11 +282,34 @@ def extra_iso(form: int) -> dict:
             "parity": parity_vs_reference(m, form)}
 
 
+def solo_seconds(probs, nt: int, tune_steps: int = 6, check=None) -> float:
+    """Device seconds of every (problem, RHS) of a batch run alone for nt steps, each with the
+    two-kernel step's autotuned z-chunk and tile height (tuned once per problem, on its first
+    RHS).  check(pid, rhs, traces) sees each solo run's seismograms."""
+    from elanfmt_gb300.solver import Solver
+
+    total = 0.0
+    for pid, (m, rl) in enumerate(probs):
+        setting = None
+        for r, (ent, coef) in enumerate(rl):
+            with Solver.from_model(m, kchunk=setting[0] if setting else 0) as s:
+                s.set_sources(ent, coef)
+                if setting is None:
+                    setting = (s.autotune(min(tune_steps, nt - 1)), s.tile())
+                s.set_tile(setting[1])
+                s.run(min(10, nt))
+                s.reset()
+                total += s.run(nt) * 1e-3
+                if check:
+                    check(pid, r, s.seismograms())
+    return total
+
+
 def extra_batch(nt: int = 300) -> dict:
     """The batched workload (6 elementary moment tensors on an orthorhombic 256^3 model + 16
     isotropic models 96^3-224^3) on a shortened run of `nt` steps: runs/s of the batched launch
     against each solve launched alone, both on the same steps."""
-    from elanfmt_gb300.solver import Batch, Solver
+    from elanfmt_gb300.solver import Batch
 
     probs = batch_workload(nt)
     runs = sum(len(r) for _, r in probs)
@@ -293,17 +318,12 @@ def extra_batch(nt: int = 300) -> dict:
         b.run(nt)
         b.reset()
         batch_s = b.run(nt) * 1e-3
-    solo_s = 0.0
-    for m, rl in probs:
-        for ent, coef in rl:
-            with Solver.from_model(m) as s:
-                s.set_sources(ent, coef)
-                s.run(min(10, nt))
-                s.reset()
-                solo_s += s.run(nt) * 1e-3
+        setting = (b.tile(),)
+    solo_s = solo_seconds(probs, nt)
     return {"workload": f"6 elementary MTs on orthorhombic 256^3 + 16 isotropic models 96^3-224^3, {nt} steps "
                         f"(the full workload runs 3000)", "runs": runs, "batched_runs_per_s": round(runs / batch_s, 3),
-            "solo_runs_per_s": round(runs / solo_s, 3), "speedup_vs_solo": round(solo_s / batch_s, 3)}
+            "solo_runs_per_s": round(runs / solo_s, 3), "speedup_vs_solo": round(solo_s / batch_s, 3),
+            "batch_tile_y": setting[0], "solo": "each run alone with its own autotuned z-chunk and tile height"}
 
 
 def extra_surrogate() -> dict:
@@ -527,15 +547,17 @@ def main_batch(args):
     import numpy as np
     import torch
 
-    from elanfmt_gb300.solver import Batch, Solver
+    from elanfmt_gb300.solver import Batch
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     nt = args.nt or 3000
-    probs = batch_workload(nt)
+    n_ortho = int(args.size.split("x")[0]) if args.size else 256
+    probs = batch_workload(nt, n_ortho=n_ortho, n_iso=args.batch_iso)
     runs = sum(len(r) for _, r in probs)
     cell_updates = sum(m.cells * len(r) for m, r in probs) * nt
     with Batch(probs) as b:
         k = b.autotune(10)
+        tile = b.tile()
         clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
         clk.start()
         ms_batch = [b.run(nt)]
@@ -545,30 +567,28 @@ def main_batch(args):
         clocks = clk.stop()
         tr0 = b.seismograms(0, 0)
     batch_s = min(ms_batch) * 1e-3
-    solo_s = 0.0
-    for pid, (m, rl) in enumerate(probs):
-        for r, (ent, coef) in enumerate(rl):
-            with Solver.from_model(m) as s:
-                s.set_sources(ent, coef)
-                s.run(min(10, nt))
-                s.reset()
-                solo_s += s.run(nt) * 1e-3
-                if pid == 0 and r == 0:
-                    assert np.array_equal(s.seismograms(), tr0), "batched and solo traces differ"
+
+    def check(pid, r, traces):
+        if pid == 0 and r == 0:
+            assert np.array_equal(traces, tr0), "batched and solo traces differ"
+
+    solo_s = solo_seconds(probs, nt, check=check)
     out = {"metric": "runs/s (batched launch vs each solve alone)", "value": round(runs / batch_s, 4),
            "unit": "runs/s", "n_gpus": 1, "steps": len(ms_batch), "higher_is_better": True,
            "solo_runs_per_s": round(runs / solo_s, 4), "speedup_vs_solo": round(solo_s / batch_s, 3),
+           "solo": "each run alone with its own autotuned z-chunk and tile height",
            "batched_gcell_updates_per_s": round(cell_updates / batch_s / 1e9, 2),
            "solo_gcell_updates_per_s": round(cell_updates / solo_s / 1e9, 2),
-           "kchunk_autotuned": k, "dtype": "f32", "data": "synthetic (seeded)",
-           "config": {"workload": f"6 elementary MTs on orthorhombic 256^3 + 16 isotropic models 96^3-224^3, {nt} steps",
+           "kchunk_autotuned": k, "tile_y_autotuned": tile, "dtype": "f32", "data": "synthetic (seeded)",
+           "config": {"workload": f"6 elementary MTs on orthorhombic {n_ortho}^3 + {args.batch_iso} isotropic models "
+                                  f"96^3-224^3, {nt} steps",
                       "runs": runs, "cell_updates": cell_updates}}
     if clocks:
         out["clocks"] = clocks
     # the reference's own kernels, one run at a time with their launch + synchronise pattern:
     # each problem's per-run rate over a bounded sample of steps, summed over the runs
-    ref_s, rates = 0.0, []
-    for m, rl in probs:
+    ref_s, rates = (None if args.no_reference else 0.0), []
+    for m, rl in (probs if ref_s is not None else []):
         r = reference_gpu(m, 100)
         if r is None:
             ref_s = None
