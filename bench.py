@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--step", default="split", choices=["split", "fused", "wave"],
                     help="step form: two kernels (default), the one-pass kernel or the wavefront launch")
     ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
+    ap.add_argument("--tile", type=int, default=0, help="CTA tile height in rows, with --kchunk (0: autotuned)")
     ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
     ap.add_argument("--batch-iso", type=int, default=16, help="batch workload: isotropic models beside the 6 MTs")
     ap.add_argument("--no-reference", action="store_true", help="batch workload: skip the reference kernels' runs")
@@ -396,6 +397,8 @@ def main():
     kchunk = args.kchunk if args.kchunk and (form != F.STEP_WAVE or args.wave_lag) else s.autotune(30)
     if form == F.STEP_WAVE and args.wave_lag:
         s.set_wave(args.wave_lag)
+    if form == F.STEP_SPLIT and args.kchunk and args.tile:
+        s.set_tile(args.tile)
 
     for _ in range(args.warmup):
         s.reset()
@@ -555,8 +558,12 @@ def main_batch(args):
     probs = batch_workload(nt, n_ortho=n_ortho, n_iso=args.batch_iso)
     runs = sum(len(r) for _, r in probs)
     cell_updates = sum(m.cells * len(r) for m, r in probs) * nt
-    with Batch(probs) as b:
-        k = b.autotune(10)
+    with Batch(probs, kchunk=args.kchunk) as b:
+        if args.kchunk and args.tile:  # a fixed setting (profiling runs)
+            k = args.kchunk
+            b.set_tile(args.tile)
+        else:
+            k = b.autotune(10)
         tile = b.tile()
         clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
         clk.start()
