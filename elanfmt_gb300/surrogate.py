@@ -381,14 +381,14 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> np.ndarray:
 
 def make_dataset(train_runs: int = 256, test_runs: int = 64, n: int = 192, nt: int = 1280, per_run: int = 64,
                  seed: int = 7, max_offset: float = 12000.0, log=print, f0: float = 0.5, decimate: int = 1,
-                 dx: float = 120.0) -> dict | None:
+                 dx: float = 120.0, pml_m: float = 1800.0) -> dict | None:
     """Runs the solver for train_runs + test_runs random source cells (depth 2-8 km, scaled to the
     grid) for nt time steps and keeps, per source, `per_run` receivers with offsets in 1 km ..
     max_offset, every `decimate`-th sample.  Under torch.distributed the sources are shared out
     over the ranks (elanfmt_gb300.runs) and only rank 0 gets the dataset (None elsewhere)."""
-    # geometry in metres (the cell counts below are those of dx = 120 m): a 1.8 km PML, receivers
-    # every 360 m, sources from 1.2 km inside the PML over 4 km
-    m = layered_iso(n=n, nt=nt, f0=f0, dx=dx, lpml=int(round(1800.0 / dx)))
+    # geometry in metres (the cell counts below are those of dx = 120 m): a pml_m (1.8 km) PML,
+    # receivers every 360 m, sources from 1.2 km inside the PML over 4 km
+    m = layered_iso(n=n, nt=nt, f0=f0, dx=dx, lpml=int(round(pml_m / dx)))
     lpml = m.meta["lpml"]
     rec_xy = surface_receivers(n, lpml, max(1, int(round(360.0 / dx))))
     rng = np.random.default_rng(seed)
@@ -594,8 +594,9 @@ def fit_and_evaluate(ds: dict, steps: int = 6000, seed: int = 7, hidden: int = 5
 def symmetry_floor(cases=((0.5, 120.0), (0.5, 60.0)), sources: int = 16, n120: int = 192, per_run: int = 64,
                    max_offset: float = 12000.0, seed: int = 9, steps_at_half_hz: int = 1280, log=print) -> list:
     """How far the solver's own traces are from the lateral symmetry that the structured surrogate
-    assumes, against grid resolution: for each (Ricker peak frequency f0, cell size dx), the
-    same physical model (n120 cells of 120 m, so n120 * 120 / dx cells), `sources` random source
+    assumes, against grid resolution and absorbing boundary: for each (Ricker peak frequency f0,
+    cell size dx[, absorbing layer thickness in metres, default 1800, and cells of 120 m added on
+    every side]), the same physical model (n120 cells of 120 m, so n120 * 120 / dx cells), `sources` random source
     cells, the 18 traces of `per_run` receivers (offset 1 km .. max_offset), and the relative L2
     residual of their best fit by 10 azimuth-independent fundamental traces (`fundamentals`),
     overall and by offset.  The window is steps_at_half_hz steps of the 120 m grid at 0.5 Hz,
@@ -603,11 +604,13 @@ def symmetry_floor(cases=((0.5, 120.0), (0.5, 60.0)), sources: int = 16, n120: i
     per wavelength are given at f0 and at 2.5 f0 (the Ricker spectrum's upper edge) for the
     slowest S velocity."""
     out = []
-    for f0, dx in cases:
-        n = int(round(n120 * 120.0 / dx))
+    for case in cases:
+        f0, dx = case[0], case[1]
+        pml_m = case[2] if len(case) > 2 else 1800.0
+        n = int(round((n120 + 2 * round((pml_m - 1800.0) / 120.0)) * 120.0 / dx))
         nt = int(round(steps_at_half_hz * (0.5 / f0) * (120.0 / dx)))
         ds = make_dataset(train_runs=sources, test_runs=0, n=n, nt=nt, per_run=per_run, seed=seed,
-                          max_offset=max_offset, log=log, f0=f0, dx=dx)
+                          max_offset=max_offset, log=log, f0=f0, dx=dx, pml_m=pml_m)
         if ds is None:
             return []
         m, Y, geo = ds["m"], ds["Y"], ds["geo"]
@@ -623,12 +626,12 @@ def symmetry_floor(cases=((0.5, 120.0), (0.5, 60.0)), sources: int = 16, n120: i
             sel = (off >= lo) & (off < hi)
             if sel.any():
                 bins[f"{lo // 1000}-{hi // 1000} km"] = {"median": float(np.median(err[sel])), "n": int(sel.sum())}
-        out.append({"f0_hz": f0, "dx_m": float(m.dx), "n": n, "steps": nt,
+        out.append({"f0_hz": f0, "dx_m": float(m.dx), "pml_m": pml_m, "n": n, "steps": nt,
                     "points_per_s_wavelength_at_f0": vs_min / f0 / m.dx,
                     "points_per_s_wavelength_at_2.5f0": vs_min / (2.5 * f0) / m.dx,
                     "gf_sets": int(live.sum()), "median": float(np.median(err)),
                     "p90": float(np.percentile(err, 90)), "by_offset": bins})
-        log(f"f0 {f0} dx {dx}: floor median {out[-1]['median']:.4f}, p90 {out[-1]['p90']:.4f}")
+        log(f"f0 {f0} dx {dx} pml {pml_m}: floor median {out[-1]['median']:.4f}, p90 {out[-1]['p90']:.4f}")
     return out
 
 
@@ -745,6 +748,7 @@ def main():
     ap.add_argument("--decimate", type=int, default=1, help="keep every d-th time step of the traces")
     ap.add_argument("--forms", default="structured", help="comma list of structured, harmonics, full")
     ap.add_argument("--floor", action="store_true", help="only the symmetry-floor study against f0")
+    ap.add_argument("--floor-cases", default="", help="f0:dx[:pml_m],... (default 0.5:120,0.25:120,0.5:60)")
     ap.add_argument("--out", default="")
     a = ap.parse_args()
     import os
@@ -783,8 +787,9 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     if a.floor:
-        res = symmetry_floor(cases=((0.5, 120.0), (0.25, 120.0), (0.5, 60.0)), n120=a.n, per_run=a.per_run,
-                             max_offset=a.max_offset)
+        cases = ((0.5, 120.0), (0.25, 120.0), (0.5, 60.0)) if not a.floor_cases else \
+            tuple(tuple(float(v) for v in c.split(":")) for c in a.floor_cases.split(","))
+        res = symmetry_floor(cases=cases, n120=a.n, per_run=a.per_run, max_offset=a.max_offset)
     else:
         res = study(a.train_runs, a.test_runs, a.n, a.nt, per_run=a.per_run, steps=a.steps, max_offset=a.max_offset,
                     decimate=a.decimate, forms=tuple(a.forms.split(",")))
