@@ -214,7 +214,10 @@ struct ewf_handle {
     int nrec = 0;
     std::vector<int32_t> h_rec;  // n*4 (i,j,k,comp)
     double *d_traces = nullptr;
-    int *d_it = nullptr;
+    int *d_it = nullptr;     // step counter: [0] (one-pass, wavefront forms); [it & 1] (two-kernel step)
+    int *d_rcol = nullptr;   // two-kernel step: first receiver entry per column (nx*ny, -1 none)
+    int4 *d_rent = nullptr;  // its entries: (k, component, trace row, next entry)
+    bool rec_fuse = true;    // the velocity kernel samples every receiver (else k_record does)
     int it = 0;
     void *d_stage = nullptr;
     size_t stage_bytes = 0;
@@ -464,6 +467,8 @@ extern "C" void ewf_destroy(ewf_handle *h)
     cudaFree(h->d_rec_comp);
     cudaFree(h->d_traces);
     cudaFree(h->d_it);
+    cudaFree(h->d_rcol);
+    cudaFree(h->d_rent);
     cudaFree(h->d_stage);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
@@ -540,8 +545,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     h->base_off = h->hx + (long long)h->sx * 1 + h->sy * 1;
     h->kchunk = p->kchunk > 0 ? p->kchunk : 16;
     h->gsteps = p->graph_steps == 0 ? 64 : (p->graph_steps < 0 ? 0 : p->graph_steps);
-    if (p->fused == EWF_STEP_FUSED && (h->gsteps & 1))
-        h->gsteps += 1;  // double-buffered graphs replay buffer pairs
+    if ((p->fused == EWF_STEP_FUSED || p->fused == EWF_STEP_SPLIT) && (h->gsteps & 1))
+        h->gsteps += 1;  // graphs replay buffer pairs (one-pass) / step-counter pairs (two-kernel step)
 
 #define CKH(call)                                                                                    \
     do {                                                                                             \
@@ -590,8 +595,8 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
             CKC(cudaMemsetAsync(h->w1[q], 0, (size_t)(n1[q] + 1) * h->esz, h->stream));
         }
     }
-    CKC(cudaMalloc(&h->d_it, sizeof(int)));
-    CKC(cudaMemsetAsync(h->d_it, 0, sizeof(int), h->stream));
+    CKC(cudaMalloc(&h->d_it, 2 * sizeof(int)));
+    CKC(cudaMemsetAsync(h->d_it, 0, 2 * sizeof(int), h->stream));
     // staging buffer for host transfers in the reference layout (largest field, FP64)
     h->stage_bytes = (size_t)(nx + 1) * (ny + 1) * (nz + 1) * 8;
     CKC(cudaMalloc(&h->d_stage, h->stage_bytes));
@@ -929,6 +934,32 @@ extern "C" int ewf_set_receivers(ewf_handle *h, int32_t n, const int32_t *ijkc)
     h->nrec = n;
     h->h_rec.assign(ijkc, ijkc + 4 * (size_t)n);
     h->graph_dirty = true;
+    // the two-kernel step's velocity kernel samples the receivers itself when every one is a
+    // velocity component on a cell its threads visit (1 <= i < nx, 1 <= j < ny, 1 <= k < nz)
+    cudaFree(h->d_rcol);
+    cudaFree(h->d_rent);
+    h->d_rcol = nullptr;
+    h->d_rent = nullptr;
+    bool fuse = true;
+    for (int r = 0; r < n; ++r) {
+        const int i = ijkc[4 * r], j = ijkc[4 * r + 1], k = ijkc[4 * r + 2], c = ijkc[4 * r + 3];
+        if (c > EWF_F_VZ || i < 1 || j < 1 || k < 1 || i >= h->p.nx || j >= h->p.ny || k >= h->p.nz) fuse = false;
+    }
+    h->rec_fuse = fuse;
+    if (fuse && n > 0) {
+        const size_t ncol = (size_t)h->p.nx * h->p.ny;
+        std::vector<int> first(ncol, -1);
+        std::vector<int4> ent((size_t)n);
+        for (int r = n - 1; r >= 0; --r) {  // chained in list order
+            const size_t col = (size_t)ijkc[4 * r] + (size_t)ijkc[4 * r + 1] * h->p.nx;
+            ent[r] = make_int4(ijkc[4 * r + 2], ijkc[4 * r + 3], r, first[col]);
+            first[col] = r;
+        }
+        CK(cudaMalloc(&h->d_rcol, ncol * sizeof(int)));
+        CK(cudaMalloc(&h->d_rent, (size_t)n * sizeof(int4)));
+        CK(cudaMemcpy(h->d_rcol, first.data(), ncol * sizeof(int), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->d_rent, ent.data(), (size_t)n * sizeof(int4), cudaMemcpyHostToDevice));
+    }
     return EWF_OK;
 }
 
@@ -947,7 +978,7 @@ extern "C" int ewf_reset(ewf_handle *h)
     h->flip = 0;
     for (auto x : h->comp_alloc) { int s = dev_zero(h, x); if (s) return s; }
     if (h->d_traces) CK(cudaMemsetAsync(h->d_traces, 0, (size_t)h->nrec * h->p.nt * sizeof(double), h->stream));
-    CK(cudaMemsetAsync(h->d_it, 0, sizeof(int), h->stream));
+    CK(cudaMemsetAsync(h->d_it, 0, 2 * sizeof(int), h->stream));
     if (h->d_wctl) {  // ticket and error flag; the generation keeps counting (stale done flags stay below it)
         CK(cudaMemsetAsync(&h->d_wctl->ticket, 0, sizeof(int), h->stream));
         CK(cudaMemsetAsync(&h->d_wctl->err, 0, sizeof(int), h->stream));
@@ -978,28 +1009,41 @@ static void launch_on(void (*kern)(P...), dim3 grid, dim3 block, cudaStream_t st
     cudaLaunchKernelEx(&cfg, kern, args...);
 }
 
+// One step of the two-kernel form; `parity` = the step number's parity: the step counter of this
+// step is d_it[parity], the next step's d_it[1 - parity].
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t *ev)
+static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t *ev, int parity)
 {
     const dim3 blk(TX, h->ty);
     const dim3 grd((h->p.nx + TX - 1) / TX, (h->p.ny + h->ty - 1) / h->ty, (h->p.nz + a.kchunk - 1) / a.kchunk);
     StressSrc ss = h->src_fuse;
     ss.stf = h->d_stf;
     ss.nstf = (int)h->nstf;
-    ss.it_ptr = h->d_it;
+    int *const it_rd = h->d_it + parity, *const it_wr = h->d_it + (1 - parity);
+    ss.it_ptr = it_rd;
     ss.order = h->p.src_order;
+    RecFuse rf{};
+    if (h->rec_fuse) {  // receivers sampled and the counter advanced by the velocity kernel
+        rf.col_first = h->d_rcol;
+        rf.ent = h->d_rent;
+        rf.traces = h->d_traces;
+        rf.trace_len = h->p.nt;
+        rf.it_rd = it_rd;
+        rf.it_wr = it_wr;
+    }
     const bool pdl = h->pdl && !ev;  // kernels timed between events run as plain launches
     if (ev) cudaEventRecord(ev[0], h->stream);
     launch_on(k_stress<T, MODEL, DAMP>, grd, blk, h->stream, pdl, a, ss);
     if (ev) cudaEventRecord(ev[1], h->stream);
     if (h->nsrc > 0 && ss.nsrc == 0)
         launch_on(k_inject<T>, dim3(1), dim3(32), h->stream, pdl, a, (const SrcEntry *)h->d_src, h->nsrc,
-                  (const double *)h->d_stf, (int)h->nstf, (const int *)h->d_it, h->p.src_order);
+                  (const double *)h->d_stf, (int)h->nstf, (const int *)it_rd, h->p.src_order);
     if (ev) cudaEventRecord(ev[2], h->stream);
-    launch_on(k_velocity<T, MODEL, DAMP, KAHAN>, grd, blk, h->stream, pdl, a);
+    launch_on(k_velocity<T, MODEL, DAMP, KAHAN>, grd, blk, h->stream, pdl, a, rf);
     if (ev) cudaEventRecord(ev[3], h->stream);
-    launch_on(k_record<T>, dim3(1), dim3(256), h->stream, pdl, a, (const long long *)h->d_rec_off,
-              (const int *)h->d_rec_comp, h->nrec, h->d_traces, (int)h->p.nt, h->d_it);
+    if (!h->rec_fuse)
+        launch_on(k_record<T>, dim3(1), dim3(256), h->stream, pdl, a, (const long long *)h->d_rec_off,
+                  (const int *)h->d_rec_comp, h->nrec, h->d_traces, (int)h->p.nt, (const int *)it_rd, it_wr);
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
@@ -1007,10 +1051,10 @@ static void launch_step_t(const ewf_handle *h, const StepArgs<T> &a, cudaEvent_t
 typedef void (*step_fn)(const ewf_handle *, cudaEvent_t *, int parity);
 
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-static void step_entry(const ewf_handle *h, cudaEvent_t *ev, int)
+static void step_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
 {
     const StepArgs<T> a = make_args<T>(h, 0);
-    launch_step_t<T, MODEL, DAMP, KAHAN>(h, a, ev);
+    launch_step_t<T, MODEL, DAMP, KAHAN>(h, a, ev, parity);
 }
 
 template <typename T, int MODEL, int DAMP, bool KAHAN>
@@ -1036,7 +1080,8 @@ static void fused_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
         cudaEventRecord(ev[2], h->stream);
         cudaEventRecord(ev[3], h->stream);
     }
-    k_record<T><<<1, 256, 0, h->stream>>>(out, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    k_record<T><<<1, 256, 0, h->stream>>>(out, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it,
+                                          h->d_it);
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
@@ -1136,7 +1181,8 @@ static void wave_entry(const ewf_handle *h, cudaEvent_t *ev, int)
         cudaEventRecord(ev[2], h->stream);
         cudaEventRecord(ev[3], h->stream);
     }
-    k_record<T><<<1, 256, 0, h->stream>>>(a, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it);
+    k_record<T><<<1, 256, 0, h->stream>>>(a, h->d_rec_off, h->d_rec_comp, h->nrec, h->d_traces, h->p.nt, h->d_it,
+                                          h->d_it);
     if (ev) cudaEventRecord(ev[4], h->stream);
 }
 
@@ -1221,6 +1267,9 @@ static int inputs_ready(const ewf_handle *h)
     return EWF_OK;
 }
 
+// The two-kernel step keeps its step counter in two alternating device locations (d_it[it & 1]).
+static bool split_form(const ewf_handle *h) { return !h->fused && !h->wave; }
+
 static int build_graph(ewf_handle *h, step_fn fn)
 {
     if (h->gexec) {
@@ -1229,7 +1278,7 @@ static int build_graph(ewf_handle *h, step_fn fn)
     }
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr, h->dbuf ? (s & 1) : 0);
+    for (int s = 0; s < h->gsteps; ++s) fn(h, nullptr, (h->dbuf || split_form(h)) ? (s & 1) : 0);
     const cudaError_t le = cudaGetLastError();
     const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -1258,7 +1307,11 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
         return ewf_fail(EWF_ERR_ARG, "source time function has %zu samples, need %d", h->nstf, h->it + nsteps);
     if ((st = step_prepare(h))) return st;
     const step_fn fn = pick_step(h);
-    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + (h->dbuf ? h->flip : 0);
+    // steps alternate a parity: the one-pass form's buffers, the two-kernel step's counter; the
+    // graph starts at parity 0
+    const bool alt = h->dbuf || split_form(h);
+    int parity = h->dbuf ? h->flip : (split_form(h) ? (h->it & 1) : 0);
+    const bool use_graph = h->gsteps > 0 && nsteps >= h->gsteps + parity;
     bool graph = use_graph;
     if (graph && (h->graph_dirty || !h->gexec)) {
         st = build_graph(h, fn);
@@ -1271,8 +1324,7 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     }
     CK(cudaEventRecord(h->ev0, h->stream));
     int done = 0;
-    int parity = h->dbuf ? h->flip : 0;
-    if (graph && parity) {  // the graph starts from buffer 0: one direct step first
+    if (graph && parity) {  // the graph starts from parity 0: one direct step first
         fn(h, nullptr, parity);
         parity = 0;
         ++done;
@@ -1288,9 +1340,9 @@ extern "C" int ewf_run(ewf_handle *h, int32_t nsteps)
     }
     for (; done < nsteps; ++done) {
         fn(h, nullptr, parity);
-        if (h->dbuf) parity ^= 1;
+        if (alt) parity ^= 1;
     }
-    h->flip = parity;
+    h->flip = h->dbuf ? parity : 0;
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -1325,7 +1377,7 @@ extern "C" int ewf_time_kernels(ewf_handle *h, int32_t nsteps, double out_ms[4])
     double acc[4] = {0, 0, 0, 0};
     int err = EWF_OK;
     for (int s = 0; s < nsteps && !err; ++s) {
-        fn(h, ev, h->flip);
+        fn(h, ev, h->dbuf ? h->flip : ((h->it + s) & 1));
         if (h->dbuf) h->flip ^= 1;
         if (cudaEventSynchronize(ev[4]) != cudaSuccess) { err = ewf_fail(EWF_ERR_CUDA, "kernel timing: %s", cudaGetErrorString(cudaGetLastError())); break; }
         for (int q = 0; q < 4; ++q) {
@@ -1354,11 +1406,11 @@ static int time_setting(ewf_handle *h, int steps, float *ms)
         return EWF_OK;
     }
     const step_fn fn = pick_step(h);
-    fn(h, nullptr, h->flip);  // warm
+    fn(h, nullptr, h->flip);  // warm (step 0 after the reset)
     if (h->dbuf) h->flip ^= 1;
     CK(cudaEventRecord(h->ev0, h->stream));
     for (int s = 0; s < steps; ++s) {
-        fn(h, nullptr, h->flip);
+        fn(h, nullptr, h->dbuf ? h->flip : ((s + 1) & 1));
         if (h->dbuf) h->flip ^= 1;
     }
     CK(cudaEventRecord(h->ev1, h->stream));
@@ -1482,7 +1534,7 @@ extern "C" int ewf_get_wave(const ewf_handle *h, int32_t *lag_pct)
 extern "C" int ewf_launches_per_step(const ewf_handle *h, int32_t *n)
 {
     if (!h || !n) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *n = (h->fused || h->wave) ? 2 : 3 + (h->nsrc > 0 && h->src_fuse.nsrc == 0 ? 1 : 0);
+    *n = (h->fused || h->wave) ? 2 : 2 + (h->nsrc > 0 && h->src_fuse.nsrc == 0 ? 1 : 0) + (h->rec_fuse ? 0 : 1);
     return EWF_OK;
 }
 
@@ -1596,8 +1648,9 @@ extern "C" int ewf_restore(ewf_handle *h, const char *path)
     }
     fclose(fp);
     if (!st) {
-        int it = hd.it;
-        if (cudaMemcpy(h->d_it, &it, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) return ewf_fail(EWF_ERR_CUDA, "restore: step copy");
+        const int it2[2] = {hd.it, hd.it};  // both counter locations (the two-kernel step reads d_it[it & 1])
+        if (cudaMemcpy(h->d_it, it2, sizeof(it2), cudaMemcpyHostToDevice) != cudaSuccess) return ewf_fail(EWF_ERR_CUDA, "restore: step copy");
+        const int it = hd.it;
         h->it = it;
     }
     return st;

@@ -81,6 +81,23 @@ struct StressSrc {
     int k1;               // last effective plane of any entry
 };
 
+// Receivers sampled by the velocity kernel itself (the two-kernel step): the thread that owns a
+// receiver's column writes the trace sample right after its update of the receiver's plane, the
+// value k_record would read (the new velocity where the update writes the cell, the old one where
+// it does not).  col_first[j*nx + i] is the first entry of the column's receivers (-1: none),
+// entries are (k, component, trace row, next entry of the column or -1).  The step counter is read
+// at it_rd and, by one thread of the launch, written plus one at it_wr (a second location, so no
+// thread of the launch can read the new value).  col_first null: k_record samples; it_wr null:
+// k_record advances the counter.
+struct RecFuse {
+    const int *col_first;
+    const int4 *ent;
+    double *traces;
+    int trace_len;
+    const int *it_rd;
+    int *it_wr;
+};
+
 // The plane after whose stores the stress kernel applies an entry.
 __host__ __device__ __forceinline__ int fused_src_plane(int comp, int k) { return (k == 1 && (comp == 7 || comp == 8)) ? 2 : k; }
 
@@ -592,8 +609,9 @@ __device__ __forceinline__ void vel_store(const StepArgs<T> &a, long long c, int
     }
 }
 
-template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, int COH = 0>
-__device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0)
+template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, int COH = 0, bool REC = false>
+__device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0,
+                                                const RecFuse &rf = RecFuse{})
 {
     constexpr bool SEP = (RC != 1) || SOFF;  // separate state and material indices (see stress_column)
     const int R = RC ? RC : a.R;
@@ -613,6 +631,12 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
     T syz_k = lds<COH>(a.f[8] + c);
     VelIn<T, MODEL, DAMP, KAHAN> nxt;
     vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c, SEP ? cm : c, k0, nxt);
+    // receivers on this column (REC: the two-kernel step's velocity kernel)
+    int r_first = -1, r_it = 0;
+    if (REC && rf.col_first) {
+        r_first = rf.col_first[(long long)j * a.nx + i];
+        if (r_first >= 0) r_it = *rf.it_rd;
+    }
 
     for (int k = k0; k < k1; ++k, c += sys) {
         if (SEP && k > k0) cm += sy;
@@ -621,6 +645,19 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
         T v[3], cp[3] = {KAHAN ? q.cp[0] : T(0), KAHAN ? q.cp[1] : T(0), KAHAN ? q.cp[2] : T(0)};
         vel_math<T, MODEL, DAMP, KAHAN>(a, q, vd, szz_m, sxz_k, syz_k, v, cp);
         vel_store<T, KAHAN>(a, c, k, i, j, v, cp);
+        if (REC && r_first >= 0 && r_it >= 0 && r_it < rf.trace_len) {
+            for (int e = r_first; e >= 0;) {
+                const int4 re = rf.ent[e];
+                if (re.x == k) {
+                    // the cell's value after the update: vel_store's ranges decide new or old
+                    const bool upd = re.y == 0 ? (j < a.ny - 1 && k < a.nz - 1)
+                                   : re.y == 1 ? (i < a.nx - 1 && k < a.nz - 1) : (i < a.nx - 1 && j < a.ny - 1);
+                    const T val = re.y == 0 ? (upd ? v[0] : q.v[0]) : re.y == 1 ? (upd ? v[1] : q.v[1]) : (upd ? v[2] : q.v[2]);
+                    rf.traces[(long long)re.z * rf.trace_len + r_it] = (double)val;
+                }
+                e = re.w;
+            }
+        }
         szz_m = q.szz;
         sxz_k = q.sxz_p;
         syz_k = q.syz_p;
@@ -628,31 +665,36 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
 }
 
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-__global__ void __launch_bounds__(split_max_threads<T>()) k_velocity(const StepArgs<T> a)
+__global__ void __launch_bounds__(split_max_threads<T>()) k_velocity(const StepArgs<T> a, const RecFuse rf)
 {
     pdl_trigger();
     pdl_wait();
+    if (rf.it_wr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *rf.it_wr = *rf.it_rd + 1;  // the next step's counter; this launch reads only it_rd
     const int k0 = blockIdx.z * a.kchunk;
-    velocity_column<T, MODEL, DAMP, KAHAN, 1>(a, blockIdx.x * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y,
-                                           k0, min(k0 + a.kchunk, a.nz));
+    velocity_column<T, MODEL, DAMP, KAHAN, 1, false, 0, true>(a, blockIdx.x * TX + threadIdx.x,
+                                                              blockIdx.y * blockDim.y + threadIdx.y, k0,
+                                                              min(k0 + a.kchunk, a.nz), 0, rf);
 }
 
 // ---------------------------------------------------------------------------------------------
 // Receiver gather (OK4:383-386, ANISO:254-268): traces[r*len + it] = field value after the
-// velocity update, widened to FP64.  One CTA; thread 0 advances the step counter last.
+// velocity update, widened to FP64.  One CTA; thread 0 advances the step counter last (it_wr =
+// it_rd + 1: the same location for the one-pass and wavefront forms, the other of the two
+// parity locations for the two-kernel step).
 // ---------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void k_record(const StepArgs<T> a, const long long *__restrict__ rec_off, const int *__restrict__ rec_comp,
-                         int nrec, double *__restrict__ traces, int trace_len, int *it_ptr)
+                         int nrec, double *__restrict__ traces, int trace_len, const int *it_rd, int *it_wr)
 {
     pdl_trigger();
     pdl_wait();
-    const int it = *it_ptr;
+    const int it = *it_rd;
     if (it >= 0 && it < trace_len)
         for (int r = threadIdx.x; r < nrec; r += blockDim.x)
             traces[(long long)r * trace_len + it] = (double)a.f[rec_comp[r]][rec_off[r]];
     __syncthreads();
-    if (threadIdx.x == 0) *it_ptr = it + 1;
+    if (threadIdx.x == 0) *it_wr = it + 1;
 }
 
 // ---------------------------------------------------------------------------------------------
