@@ -83,6 +83,15 @@ def workload(name: str, nt: int, size: str):
     return m, desc
 
 
+def workload_config(m, desc: str, world: int) -> dict:
+    """The `config` of a bench line: what the workload is, the same for both arms."""
+    ws = m.cells * 4 * 21  # 9 state + 12 material fields, FP32
+    return {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": m.nt, "receivers": len(m.receivers),
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": ("inputs larger than L2 (working set ~%.1f GB)" % (ws / 1e9)) if ws > 129e6 else
+                  ("working set ~%.0f MB, within L2 (no flush between runs)" % (ws / 1e6))}
+
+
 class Clocks:
     """nvidia-smi sampled every 200 ms while the timed region runs."""
 
@@ -424,12 +433,10 @@ def main():
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": nt, "receivers": len(m.receivers),
-                   "kchunk_autotuned": kchunk, "step": args.step,
+        "config": workload_config(m, desc, world),
+        "tuning": {"step": args.step, "kchunk_autotuned": kchunk,
                    **({"tile_y_autotuned": s.tile()} if form == F.STEP_SPLIT else {}),
-                   **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {}),
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "inputs larger than L2 (working set ~%.1f GB)" % (m.cells * 4 * 21 / 1e9)},
+                   **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {})},
         "gpu_launches": launches,
     }
     step_frac = value * STEP_BYTES[args.workload] / peak
@@ -638,7 +645,7 @@ def main_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic (seeded)", "config": {"workload": desc, "grid": [m.nx, m.ny, m.nz], "nt": m.nt},
+           "data": "synthetic (seeded)", "config": workload_config(m, desc, args.gpus),
            "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": O.num_threads(), "kind": "port",
                             "sample": sample},
            "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
