@@ -228,6 +228,7 @@ struct ewf_handle {
     int kchunk = 32;
     int ty = TY;        // two-kernel step: CTA tile height in rows (autotuned)
     bool pdl = true;    // two-kernel step: kernels launched as programmatic dependents (off if capture refuses)
+    int l2pf = 0;       // two-kernel step: L2 prefetch distance of the velocity kernel in planes (autotuned)
     bool fdiv = false;  // div_spacing verified for (float) dx, dy, dz
     struct Snapshots *snap = nullptr;  // queued snapshot writer (created on first use)
 };
@@ -368,6 +369,7 @@ static StepArgs<T> make_args(const ewf_handle *h, int which = -1)
     a.bz = (T)h->p.bz;
     a.third = (T)1.0 / (T)3.0;
     a.fdiv = h->fdiv ? 1 : 0;
+    a.l2pf = h->l2pf;
     a.vdamp = (T)h->p.vdamp;
     a.bc1 = h->p.free_surface == EWF_FS_BC1 ? 1 : 0;
     a.smu_on = h->p.surface_mu > 0.0 ? 1 : 0;
@@ -1478,6 +1480,22 @@ extern "C" int ewf_set_tile(ewf_handle *h, int32_t tile_y)
         return ewf_fail(EWF_ERR_ARG, "tile_y must be a power of two in [1, %d] (got %d)", mx, tile_y);
     h->ty = tile_y;
     h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_l2_prefetch(ewf_handle *h, int32_t planes)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (planes < 0 || planes > 8) return ewf_fail(EWF_ERR_ARG, "planes must be in [0, 8] (got %d)", planes);
+    h->l2pf = planes;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_l2_prefetch(const ewf_handle *h, int32_t *planes)
+{
+    if (!h || !planes) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *planes = h->l2pf;
     return EWF_OK;
 }
 

@@ -58,6 +58,7 @@ struct StepArgs {
     int bc1;            // 1: BC1 after the stress update (stress_store, inject_entry); 0: none
     int smu_on;         // isotropic 1-D PML scheme: shear modulus smu instead of c66 on plane k = 1
     T smu;
+    int l2pf;           // two-kernel step: the velocity kernel asks L2 for its inputs this many planes ahead (0: off)
 };
 
 struct SrcEntry {
@@ -609,6 +610,22 @@ __device__ __forceinline__ void vel_store(const StepArgs<T> &a, long long c, int
     }
 }
 
+// L2 prefetch of plane-ahead inputs of the velocity update for one warp's row of 32 cells: lane l
+// asks for the 128-byte line of input field l (sxx..syz, Vx..Vz, then buoyancy, 3-D weights and
+// compensation where the scheme reads them) that holds the row's cells; c is this lane's
+// element, so c - lane is the row's first (the x pitch and the row start are 32-aligned).
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+__device__ __forceinline__ void vel_prefetch_row(const StepArgs<T> &a, long long c, int lane)
+{
+    const T *p = nullptr;
+    if (lane < 6) p = a.f[3 + lane];
+    else if (lane < 9) p = a.f[lane - 6];
+    else if (MODEL != MODEL_ISO && lane < 12) p = a.m[lane];
+    else if (MODEL != MODEL_ISO && DAMP == DAMP_W3D && lane == 12) p = a.w3;
+    else if (KAHAN && lane >= 13 && lane < 16) p = a.comp[lane - 13];
+    if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + (c - lane)));
+}
+
 template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, int COH = 0, bool REC = false>
 __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int j, int kc0, int kc1, long long soff = 0,
                                                 const RecFuse &rf = RecFuse{})
@@ -642,6 +659,8 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
         if (SEP && k > k0) cm += sy;
         VelIn<T, MODEL, DAMP, KAHAN> q = nxt;
         if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
+        if (REC && a.l2pf > 0 && k + a.l2pf < k1)
+            vel_prefetch_row<T, MODEL, DAMP, KAHAN>(a, c + (long long)a.l2pf * sys, (int)threadIdx.x);
         T v[3], cp[3] = {KAHAN ? q.cp[0] : T(0), KAHAN ? q.cp[1] : T(0), KAHAN ? q.cp[2] : T(0)};
         vel_math<T, MODEL, DAMP, KAHAN>(a, q, vd, szz_m, sxz_k, syz_k, v, cp);
         vel_store<T, KAHAN>(a, c, k, i, j, v, cp);

@@ -78,6 +78,8 @@ SIGNATURES = {
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_dependent_launch": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_set_l2_prefetch": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_get_l2_prefetch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_get_dependent_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_wave_hold": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -296,6 +298,15 @@ class Solver:
         ty = C.c_int32()
         _check(self._lib.ewf_get_tile(self._h, C.byref(ty)), "ewf_get_tile")
         return ty.value
+
+    def set_l2_prefetch(self, planes: int) -> None:
+        """Two-kernel step: L2 prefetch distance of the velocity kernel (0 = off; results do not depend on it)."""
+        _check(self._lib.ewf_set_l2_prefetch(self._h, int(planes)), "ewf_set_l2_prefetch")
+
+    def l2_prefetch(self) -> int:
+        v = C.c_int32()
+        _check(self._lib.ewf_get_l2_prefetch(self._h, C.byref(v)), "ewf_get_l2_prefetch")
+        return v.value
 
     def set_dependent_launch(self, on: bool) -> None:
         """Two-kernel step: programmatic dependent launches (default on; results do not depend on it)."""

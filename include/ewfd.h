@@ -224,6 +224,10 @@ int ewf_get_tile(const ewf_handle *h, int32_t *tile_y);
  * Results do not depend on it. */
 int ewf_set_dependent_launch(ewf_handle *h, int32_t on);
 int ewf_get_dependent_launch(const ewf_handle *h, int32_t *on);
+/* Two-kernel step: the velocity kernel asks L2 for the input lines of the plane `planes` ahead
+ * (0..8; 0 = off, the default).  A hint: results do not depend on it. */
+int ewf_set_l2_prefetch(ewf_handle *h, int32_t planes);
+int ewf_get_l2_prefetch(const ewf_handle *h, int32_t *planes);
 
 /* Wavefront step (fused = EWF_STEP_WAVE): the lag of the velocity items behind the stress items
  * in percent of the resident CTAs, 1..100000 (set by ewf_autotune; results do not depend on it).

@@ -256,7 +256,8 @@ def test_split_tile_heights(cuda_device, prec):
         for ty in heights:
             with Solver.from_model(m, precision=prec, kchunk=6, graph_steps=4) as s:
                 s.set_tile(ty)
-                assert s.tile() == ty
+                s.set_l2_prefetch(ty % 5)  # the L2 hint off and on (1-4 planes ahead)
+                assert s.tile() == ty and s.l2_prefetch() == ty % 5
                 s.run(20)
                 got = ([s.field(q, dt) for q in F.STATE], s.seismograms())
             assert_bitwise(got, ref, f"model {model} tile height {ty}")
