@@ -61,6 +61,7 @@ def parse():
                     help="step form: two kernels (default), the one-pass kernel or the wavefront launch")
     ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
     ap.add_argument("--tile", type=int, default=0, help="CTA tile height in rows, with --kchunk (0: autotuned)")
+    ap.add_argument("--l2pf", type=int, default=0, help="velocity kernel's L2 prefetch distance, with --kchunk --tile")
     ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
     ap.add_argument("--batch-iso", type=int, default=16, help="batch workload: isotropic models beside the 6 MTs")
     ap.add_argument("--no-reference", action="store_true", help="batch workload: skip the reference kernels' runs")
@@ -274,7 +275,7 @@ def extra_iso(form: int) -> dict:
     m, desc = workload("iso", 0, "")
     with Solver.from_model(m, fused=form) as s:
         kchunk = s.autotune(20)
-        tile = s.tile() if form == F.STEP_SPLIT else None
+        tile = (s.tile(), s.l2_prefetch()) if form == F.STEP_SPLIT else None
         s.reset()
         s.run(m.nt)
         ms = []
@@ -285,7 +286,8 @@ def extra_iso(form: int) -> dict:
     value = m.cells * m.nt / (best * 1e-3) / 1e9
     peak, kind = peaks()
     return {"workload": desc, "value": round(value, 3), "unit": UNIT, "ms_per_run": round(best, 3), "runs": len(ms),
-            "kchunk_autotuned": kchunk, **({"tile_y_autotuned": tile} if tile else {}),
+            "kchunk_autotuned": kchunk,
+            **({"tile_y_autotuned": tile[0], "l2_prefetch_autotuned": tile[1]} if tile else {}),
             "step_roofline": {"bytes_per_cell": STEP_BYTES["iso"], "achieved": round(value * STEP_BYTES["iso"], 1),
                               "peak": peak, "unit": "GB/s", "frac": round(value * STEP_BYTES["iso"] / peak, 4),
                               "peak_kind": kind},
@@ -294,8 +296,8 @@ def extra_iso(form: int) -> dict:
 
 def solo_seconds(probs, nt: int, tune_steps: int = 6, check=None) -> float:
     """Device seconds of every (problem, RHS) of a batch run alone for nt steps, each with the
-    two-kernel step's autotuned z-chunk and tile height (tuned once per problem, on its first
-    RHS).  check(pid, rhs, traces) sees each solo run's seismograms."""
+    two-kernel step's autotuned z-chunk, tile height and L2 prefetch (tuned once per problem, on
+    its first RHS).  check(pid, rhs, traces) sees each solo run's seismograms."""
     from elanfmt_gb300.solver import Solver
 
     total = 0.0
@@ -305,8 +307,9 @@ def solo_seconds(probs, nt: int, tune_steps: int = 6, check=None) -> float:
             with Solver.from_model(m, kchunk=setting[0] if setting else 0) as s:
                 s.set_sources(ent, coef)
                 if setting is None:
-                    setting = (s.autotune(min(tune_steps, nt - 1)), s.tile())
+                    setting = (s.autotune(min(tune_steps, nt - 1)), s.tile(), s.l2_prefetch())
                 s.set_tile(setting[1])
+                s.set_l2_prefetch(setting[2])
                 s.run(min(10, nt))
                 s.reset()
                 total += s.run(nt) * 1e-3
@@ -408,6 +411,7 @@ def main():
         s.set_wave(args.wave_lag)
     if form == F.STEP_SPLIT and args.kchunk and args.tile:
         s.set_tile(args.tile)
+        s.set_l2_prefetch(args.l2pf)
 
     for _ in range(args.warmup):
         s.reset()
@@ -435,7 +439,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": workload_config(m, desc, world),
         "tuning": {"step": args.step, "kchunk_autotuned": kchunk,
-                   **({"tile_y_autotuned": s.tile()} if form == F.STEP_SPLIT else {}),
+                   **({"tile_y_autotuned": s.tile(), "l2_prefetch_autotuned": s.l2_prefetch()}
+                      if form == F.STEP_SPLIT else {}),
                    **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {})},
         "gpu_launches": launches,
     }

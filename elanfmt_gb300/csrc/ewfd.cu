@@ -1466,6 +1466,24 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     h->kchunk = best_k;
     h->ty = best_ty;
     h->wave_lag_pct = best_lag;
+    if (split) {  // then the velocity kernel's L2 prefetch distance at that setting
+        int best_pf = 0;
+        h->l2pf = 0;
+        float base = 0.f;
+        if ((st = time_setting(h, steps, &base))) return st;
+        best = base;
+        static const int pf_cand[] = {2, 3, 4};
+        for (int pf : pf_cand) {
+            h->l2pf = pf;
+            float ms = 0.f;
+            if ((st = time_setting(h, steps, &ms))) return st;
+            if (ms >= 0.f && ms < best) {
+                best = ms;
+                best_pf = pf;
+            }
+        }
+        h->l2pf = best_pf;
+    }
     h->graph_dirty = true;
     if (kchunk) *kchunk = best_k;
     return ewf_reset(h);

@@ -341,6 +341,9 @@ __device__ __forceinline__ void stress_store(const StepArgs<T> &a, long long c, 
     }
 }
 
+// L2 prefetch of one 128-byte line (a hint: no completion to wait for, no register written).
+__device__ __forceinline__ void l2_prefetch_line(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // The column (X = i*R + r, j) over planes [k0, k1): X runs over the cells of every RHS.
 // RC: R known at compile time (1: one RHS, state and materials share one index; 0: a.R).
 // SOFF (with RC = 1): the state lives soff elements after the materials' index (one of several
@@ -612,18 +615,20 @@ __device__ __forceinline__ void vel_store(const StepArgs<T> &a, long long c, int
 
 // L2 prefetch of plane-ahead inputs of the velocity update for one warp's row of 32 cells: lane l
 // asks for the 128-byte line of input field l (sxx..syz, Vx..Vz, then buoyancy, 3-D weights and
-// compensation where the scheme reads them) that holds the row's cells; c is this lane's
-// element, so c - lane is the row's first (the x pitch and the row start are 32-aligned).
+// compensation where the scheme reads them) that holds the row's cells.  This returns lane l's
+// field (null: none); the row's line of plane k is at field + (c - lane) + k * plane pitch, c
+// being the lane's element (the x pitch and the row start are 32-aligned).  (The stress kernel,
+// already at the copy bandwidth, has no registers to spare for it.)
 template <typename T, int MODEL, int DAMP, bool KAHAN>
-__device__ __forceinline__ void vel_prefetch_row(const StepArgs<T> &a, long long c, int lane)
+__device__ __forceinline__ const T *vel_prefetch_field(const StepArgs<T> &a, int lane)
 {
-    const T *p = nullptr;
-    if (lane < 6) p = a.f[3 + lane];
-    else if (lane < 9) p = a.f[lane - 6];
-    else if (MODEL != MODEL_ISO && lane < 12) p = a.m[lane];
-    else if (MODEL != MODEL_ISO && DAMP == DAMP_W3D && lane == 12) p = a.w3;
-    else if (KAHAN && lane >= 13 && lane < 16) p = a.comp[lane - 13];
-    if (p) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + (c - lane)));
+    if (lane < 6) return a.f[3 + lane];
+    if (lane < 9) return a.f[lane - 6];
+    if (MODEL != MODEL_ISO && lane < 12) return a.m[lane];
+    if (MODEL != MODEL_ISO && DAMP == DAMP_W3D && lane == 12) return a.w3;
+    if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP && lane >= 9 && lane < 12) return a.w6[lane - 9];
+    if (KAHAN && lane >= 13 && lane < 16) return a.comp[lane - 13];
+    return nullptr;
 }
 
 template <typename T, int MODEL, int DAMP, bool KAHAN, int RC, bool SOFF = false, int COH = 0, bool REC = false>
@@ -648,6 +653,12 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
     T syz_k = lds<COH>(a.f[8] + c);
     VelIn<T, MODEL, DAMP, KAHAN> nxt;
     vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c, SEP ? cm : c, k0, nxt);
+    // the L2 prefetch's field for this lane (REC: the two-kernel step's velocity kernel)
+    const T *pf_row = nullptr;
+    if (REC && a.l2pf > 0) {
+        pf_row = vel_prefetch_field<T, MODEL, DAMP, KAHAN>(a, (int)threadIdx.x);
+        if (pf_row) pf_row += c - (long long)threadIdx.x + (long long)a.l2pf * sys;
+    }
     // receivers on this column (REC: the two-kernel step's velocity kernel)
     int r_first = -1, r_it = 0;
     if (REC && rf.col_first) {
@@ -659,8 +670,7 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
         if (SEP && k > k0) cm += sy;
         VelIn<T, MODEL, DAMP, KAHAN> q = nxt;
         if (k + 1 < k1) vel_load<T, MODEL, DAMP, KAHAN, RC, COH>(a, c + sys, SEP ? cm + sy : c + sys, k + 1, nxt);
-        if (REC && a.l2pf > 0 && k + a.l2pf < k1)
-            vel_prefetch_row<T, MODEL, DAMP, KAHAN>(a, c + (long long)a.l2pf * sys, (int)threadIdx.x);
+        if (REC && pf_row && k + a.l2pf < k1) l2_prefetch_line(pf_row + (long long)(k - k0) * sys);
         T v[3], cp[3] = {KAHAN ? q.cp[0] : T(0), KAHAN ? q.cp[1] : T(0), KAHAN ? q.cp[2] : T(0)};
         vel_math<T, MODEL, DAMP, KAHAN>(a, q, vd, szz_m, sxz_k, syz_k, v, cp);
         vel_store<T, KAHAN>(a, c, k, i, j, v, cp);

@@ -10,9 +10,10 @@ on the inputs' values, so it is stored under that key (the wavefront form's lag 
     k = tuning.kchunk_for(model, precision=F.PREC_F32)      # cached, or tuned once and stored
     with Solver.from_model(model, kchunk=k) as s: ...
 
-    k, ty = tuning.split_setting_for(model)                 # z-chunk and tile height
+    k, ty, pf = tuning.split_setting_for(model)             # z-chunk, tile height, L2 prefetch
     with Solver.from_model(model, kchunk=k) as s:
         s.set_tile(ty)
+        s.set_l2_prefetch(pf)
 
 The cache file defaults to $EWF_TUNING_CACHE or ~/.cache/elanfmt_gb300/kchunk.json.
 """
@@ -87,10 +88,10 @@ def kchunk_for(m, precision: int = F.PREC_F32, fused: int = F.STEP_SPLIT, nsteps
 
 
 def split_setting_for(m, precision: int = F.PREC_F32, nsteps: int = 30, path: str | None = None,
-                      device_name: str | None = None, tune=None) -> tuple[int, int]:
-    """The two-kernel step's cached (z-chunk, tile height) for this workload shape, or the
-    autotuner's choice (then cached).  `tune(m, precision, nsteps) -> (kchunk, tile_y)` replaces
-    the GPU autotuner (tests)."""
+                      device_name: str | None = None, tune=None) -> tuple[int, int, int]:
+    """The two-kernel step's cached (z-chunk, tile height, L2 prefetch distance) for this workload
+    shape, or the autotuner's choice (then cached).  `tune(m, precision, nsteps) -> (kchunk,
+    tile_y, l2_prefetch)` replaces the GPU autotuner (tests)."""
     if device_name is None:
         import torch
 
@@ -98,15 +99,15 @@ def split_setting_for(m, precision: int = F.PREC_F32, nsteps: int = 30, path: st
     k = key(device_name, m, precision, F.STEP_SPLIT) + "|tile"
     data = load(path)
     v = data.get(k)
-    if isinstance(v, list) and len(v) == 2:
-        return int(v[0]), int(v[1])
+    if isinstance(v, list) and len(v) == 3:
+        return int(v[0]), int(v[1]), int(v[2])
     if tune is None:
         from .solver import Solver
 
         def tune(m_, p_, n_):
             with Solver.from_model(m_, precision=p_) as s:
-                return s.autotune(n_), s.tile()
+                return s.autotune(n_), s.tile(), s.l2_prefetch()
 
-    kc, ty = (int(x) for x in tune(m, precision, nsteps))
-    store(k, [kc, ty], path)
-    return kc, ty
+    kc, ty, pf = (int(x) for x in tune(m, precision, nsteps))
+    store(k, [kc, ty, pf], path)
+    return kc, ty, pf

@@ -208,8 +208,8 @@ int ewf_launches_per_step(const ewf_handle *h, int32_t *n);
 
 /* Autotuner: times `nsteps` steps for each z-chunk candidate (planes per CTA) with CUDA events,
  * keeps the fastest (returned in *kchunk, may be NULL) and resets the state.  The two-kernel step
- * also tunes its tile height (4, 8, 16 rows; ewf_get_tile), the wavefront step its lag (both kept
- * in the handle). */
+ * also tunes its tile height (4, 8, 16 rows; ewf_get_tile) and then its L2 prefetch distance
+ * (0, 2, 3, 4 planes; ewf_get_l2_prefetch), the wavefront step its lag (all kept in the handle). */
 int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
 
 /* Two-kernel step (fused = EWF_STEP_SPLIT): the height of a CTA's tile in rows of 32 columns
@@ -225,7 +225,7 @@ int ewf_get_tile(const ewf_handle *h, int32_t *tile_y);
 int ewf_set_dependent_launch(ewf_handle *h, int32_t on);
 int ewf_get_dependent_launch(const ewf_handle *h, int32_t *on);
 /* Two-kernel step: the velocity kernel asks L2 for the input lines of the plane `planes` ahead
- * (0..8; 0 = off, the default).  A hint: results do not depend on it. */
+ * (0..8; 0 = off, the default; ewf_autotune picks it).  A hint: results do not depend on it. */
 int ewf_set_l2_prefetch(ewf_handle *h, int32_t planes);
 int ewf_get_l2_prefetch(const ewf_handle *h, int32_t *planes);
 

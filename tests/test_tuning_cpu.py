@@ -41,15 +41,15 @@ def test_split_setting_cached_with_tile_height(tmp_path):
 
     def fake(m, prec, n):
         calls.append((m.nx, prec))
-        return (8, 16) if m.nx == 20 else (24, 4)
+        return (8, 16, 3) if m.nx == 20 else (24, 4, 0)
 
     a = I.random_small(F.MODEL_ORTHO, 20, 18, 16, nt=5, seed=1)
     b = I.random_small(F.MODEL_ISO, 24, 18, 16, nt=5, seed=1)
-    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16)
-    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16)
-    assert tuning.split_setting_for(b, path=path, device_name="gpuX", tune=fake) == (24, 4)
+    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16, 3)
+    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16, 3)
+    assert tuning.split_setting_for(b, path=path, device_name="gpuX", tune=fake) == (24, 4, 0)
     assert len(calls) == 2
     # the z-chunk-only entries of the same shape stay separate
     assert tuning.kchunk_for(a, path=path, device_name="gpuX", tune=lambda *x: 12) == 12
-    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16)
-    assert sorted(len(v) if isinstance(v, list) else 1 for v in tuning.load(path).values()) == [1, 2, 2]
+    assert tuning.split_setting_for(a, path=path, device_name="gpuX", tune=fake) == (8, 16, 3)
+    assert sorted(len(v) if isinstance(v, list) else 1 for v in tuning.load(path).values()) == [1, 3, 3]
