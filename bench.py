@@ -633,7 +633,7 @@ def main_reference(args):
     t = time.perf_counter()
     r.step(1)
     one = time.perf_counter() - t
-    per = max(1, min(20, int(6.0 / max(one, 1e-6))))
+    per = max(1, min(20, int(6.0 / max(one, 1e-6)), m.nt - 2))  # a sample never runs past nt
     for _ in range(args.warmup):
         r.step(per) if r.state.it + per < m.nt else None
     times = []
