@@ -75,7 +75,7 @@ def workload(name: str, nt: int, size: str):
         nx, ny, nz = (int(v) for v in size.split("x")) if size else (320, 320, 256)
         m = I.ortho_layered(nx=nx, ny=ny, nz=nz, nt=nt or 4000, src=(nx // 2, ny // 2, nz // 2),
                             rec_coords=None if (nx, ny) == (320, 320) else
-                            [int(round(v)) for v in (nx * (0.125 + 0.75 * q / 7) for q in range(8))])
+                            [int(round(v)) for v in (min(nx, ny) * (0.125 + 0.75 * q / 7) for q in range(8))])
         desc = f"orthorhombic layered {nx}x{ny}x{nz}, {m.nt} steps, 12 layers, 15-cell PML, lune MT, Ricker 1.5 Hz"
     else:
         n = int(size.split("x")[0]) if size else 128
