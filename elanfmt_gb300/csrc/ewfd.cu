@@ -398,9 +398,6 @@ __global__ void k_fdiv_check(float d, float r, unsigned *bad)
 }
 }  // namespace ewf
 
-// The FP64 division path's spacing range (div_spacing(double) checks every quotient it returns).
-bool ewf_ddiv_spacing_ok(double d) { return d >= 0x1p-100 && d <= 0x1p100; }
-
 bool ewf_fdiv_verified(float d)
 {
     if (!(d >= 0x1p-10f && d <= 0x1p30f)) return false;
@@ -582,8 +579,6 @@ extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
     }
     if (p->model == EWF_MODEL_ORTHO && h->esz == 4)
         h->fdiv = ewf_fdiv_verified((float)p->dx) && ewf_fdiv_verified((float)p->dy) && ewf_fdiv_verified((float)p->dz);
-    if (p->model == EWF_MODEL_ORTHO && h->esz == 8)  // each FP64 quotient checks itself; the spacings gate it
-        h->fdiv = ewf_ddiv_spacing_ok(p->dx) && ewf_ddiv_spacing_ok(p->dy) && ewf_ddiv_spacing_ok(p->dz);
     for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->f_alloc[q]));
     if (h->dbuf)
         for (int q = 0; q < 9; ++q) CKH(alloc_box(h, &h->g_alloc[q]));

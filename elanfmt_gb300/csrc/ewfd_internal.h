@@ -15,6 +15,5 @@ const double *ewf_stf_host_copy(const ewf_handle *h, std::vector<double> &out);
 // True when div_spacing's reciprocal path (ewfd_kernels.cuh) reproduces IEEE division by the
 // float spacing d on the current device (checked once per device and value, then cached).
 bool ewf_fdiv_verified(float d);
-bool ewf_ddiv_spacing_ok(double d);
 // Writes `bytes` raw bytes to path (status code; message via ewf_last_error on failure).
 int ewf_write_raw_file(const char *path, const void *data, size_t bytes);

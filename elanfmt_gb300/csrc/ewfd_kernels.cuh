@@ -152,32 +152,7 @@ __device__ __forceinline__ float div_spacing(float x, float d, float r, bool ok)
     }
     return __fdiv_rn(x, d);
 }
-// FP64: the same correction step, but each result is checked before it is used, so no per-spacing
-// verification is needed (a binade of doubles cannot be enumerated).  With r = RN(1/d),
-// q0 = RN(x r), q1 = RN(q0 + (x - q0 d) r), the residual t = x - q1 d is exactly representable
-// whenever |t| <= ulp(q1)|d| (x and q1 d are multiples of ulp(q1) ulp(d) and t then needs at most
-// 53 bits), so e1 = RN(t) from one FMA is exact there and larger otherwise.  q1 is RN(x/d) if
-// |x/d - q1| is below half the spacing of doubles around q1: |e1| < ulp(q1)/2 |d| (ulp(q1)/4 |d|
-// when q1 is a power of two, whose lower neighbour is half as far), a product with a power of two,
-// hence exact.  A result that fails the test (or a tie) takes IEEE division.  The range gate
-// (2^-800 <= |x| <= 2^800, and 2^-100 <= d <= 2^100 on the host: `ok`) keeps every quantity
-// normal.
-__device__ __forceinline__ double div_spacing(double x, double d, double r, bool ok)
-{
-    const unsigned long long ax = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-    if (ok && ax - 0x0df0000000000000ull <= 0x71f0000000000000ull - 0x0df0000000000000ull) {  // 2^-800 .. 2^800
-        const double q0 = __dmul_rn(x, r);
-        const double e0 = __fma_rn(-q0, d, x);
-        const double q1 = __fma_rn(e0, r, q0);
-        const double e1 = __fma_rn(-q1, d, x);
-        const unsigned long long bq = (unsigned long long)__double_as_longlong(q1) & 0x7fffffffffffffffull;
-        const long long eq = (long long)(bq >> 52);                       // biased exponent of q1
-        const long long eh = eq - 53 - ((bq & 0xfffffffffffffull) == 0);  // ulp(q1)/2, or /4 at a power of two
-        const double T = __dmul_rn(__longlong_as_double(eh << 52), fabs(d));
-        if (fabs(e1) < T) return q1;
-    }
-    return x / d;
-}
+__device__ __forceinline__ double div_spacing(double x, double d, double, bool) { return x / d; }
 
 // ---------------------------------------------------------------------------------------------
 // Stress update.  Isotropic: OK4:285-331.  Orthorhombic: ANISO:287-356.  BC1: OK4:271-283.
