@@ -36,7 +36,9 @@ def errors(a: np.ndarray, ref: np.ndarray) -> dict:
             "peak_err_median": float(np.median(peak)), "rel_l2_per_trace": [float(v) for v in l2]}
 
 
-def study(n: int = 256, nt: int = 6000) -> dict:
+def study(n: int = 256, nt: int = 6000, tune: bool = True) -> dict:
+    """The three runs (each form with its autotuned launch setting unless tune is False) and the
+    FP32 forms' errors against FP64."""
     m = I.ortho_layered(nx=n, ny=n, nz=n, nt=nt, src=(n // 2, n // 2, n // 2),
                         rec_coords=[int(round(v)) for v in (n * (0.125 + 0.75 * q / 7) for q in range(8))])
     out = {"model": f"orthorhombic layered {n}^3 (12-layer table of the 320x320x256 workload), {nt} steps",
@@ -44,6 +46,8 @@ def study(n: int = 256, nt: int = 6000) -> dict:
     traces = {}
     for name, prec in (("fp64", F.PREC_F64), ("fp32", F.PREC_F32), ("fp32_kahan", F.PREC_F32_KAHAN)):
         with Solver.from_model(m, precision=prec) as s:
+            if tune:
+                s.autotune(min(10, nt - 1))
             t = time.perf_counter()
             ms = s.run(nt)
             traces[name] = s.seismograms()
