@@ -9,6 +9,7 @@
 #include "ewfd_internal.h"
 #include "ewfd_kernels.cuh"
 #include "ewfd_fused.cuh"
+#include "ewfd_band.h"
 #include "ewfd_wave.cuh"
 
 #include <algorithm>
@@ -182,6 +183,7 @@ struct ewf_handle {
     void *f_alloc[9] = {};
     void *g_alloc[9] = {};  // second state buffer of the fused step
     bool fused = false;
+    int band = 0;           // one-pass step: rows per band CTA of the cluster kernel (k_band); 0: k_step
     bool dbuf = false;      // double-buffered state (one-pass step)
     int flip = 0;           // double-buffered: the current state is in g_alloc when 1
     bool wave = false;      // wavefront step (ewfd_wave.cuh)
@@ -519,6 +521,8 @@ static int validate_params(const ewf_params *p)
         return ewf_fail(EWF_ERR_UNSUPPORTED, "the one-pass step applies BC1 and the plain shear modulus only");
     return EWF_OK;
 }
+
+static bool band_fits(const ewf_handle *h, int rows);
 
 extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
 {
@@ -1073,10 +1077,14 @@ static void fused_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
     fa.nstf = (int)h->nstf;
     fa.it_ptr = h->d_it;
     fa.order = h->p.src_order;
-    const dim3 blk(FX, FY);
-    const dim3 grd((h->p.nx + FX - 1) / FX, (h->p.ny + FY - 1) / FY, (h->p.nz + fa.a.kchunk - 1) / fa.a.kchunk);
     if (ev) cudaEventRecord(ev[0], h->stream);
-    k_step<T, MODEL, DAMP, KAHAN><<<grd, blk, 0, h->stream>>>(fa);
+    if (h->band > 0) {
+        band_launch<T, MODEL, DAMP, KAHAN>(fa, h->band, band_grid(h->p.nx, h->p.ny, h->p.nz, h->band, fa.a.kchunk), h->stream);
+    } else {
+        const dim3 blk(FX, FY);
+        const dim3 grd((h->p.nx + FX - 1) / FX, (h->p.ny + FY - 1) / FY, (h->p.nz + fa.a.kchunk - 1) / fa.a.kchunk);
+        k_step<T, MODEL, DAMP, KAHAN><<<grd, blk, 0, h->stream>>>(fa);
+    }
     if (ev) {
         cudaEventRecord(ev[1], h->stream);
         cudaEventRecord(ev[2], h->stream);
@@ -1232,6 +1240,39 @@ static step_fn pick_step_t(const ewf_params &p)
     default:
         if (iso) return entry<FORM, double, MODEL_ISO, DAMP_PML1D, false>();
         return w3 ? entry<FORM, double, MODEL_ORTHO, DAMP_W3D, false>() : entry<FORM, double, MODEL_ORTHO, DAMP_SEP, false>();
+    }
+}
+
+// Can the band kernel of the one-pass step run with `rows` rows per CTA on this handle's grid
+// (built for the element type, at most BAND_MAX_CTAS CTAs per band, a cluster fits the device)?
+template <typename T, int MODEL, int DAMP, bool KAHAN>
+static bool band_fits_t(const ewf_handle *h, int rows)
+{
+    if (!band_rows_built<T>(rows)) return false;
+    int n = 0;
+    const cudaError_t e = band_clusters<T, MODEL, DAMP, KAHAN>(rows, band_grid(h->p.nx, h->p.ny, h->p.nz, rows, h->kchunk), &n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n >= 1;
+}
+
+static bool band_fits(const ewf_handle *h, int rows)
+{
+    const ewf_params &p = h->p;
+    if (!h->fused || p.damping == EWF_DAMP_PERCOMP || p.model == EWF_MODEL_ISO_HET) return false;
+    const bool iso = p.model == EWF_MODEL_ISO, w3 = p.damping == EWF_DAMP_W3D;
+    switch (p.precision) {
+    case EWF_PREC_F32:
+        if (iso) return band_fits_t<float, MODEL_ISO, DAMP_PML1D, false>(h, rows);
+        return w3 ? band_fits_t<float, MODEL_ORTHO, DAMP_W3D, false>(h, rows) : band_fits_t<float, MODEL_ORTHO, DAMP_SEP, false>(h, rows);
+    case EWF_PREC_F32_KAHAN:
+        if (iso) return band_fits_t<float, MODEL_ISO, DAMP_PML1D, true>(h, rows);
+        return w3 ? band_fits_t<float, MODEL_ORTHO, DAMP_W3D, true>(h, rows) : band_fits_t<float, MODEL_ORTHO, DAMP_SEP, true>(h, rows);
+    default:
+        if (iso) return band_fits_t<double, MODEL_ISO, DAMP_PML1D, false>(h, rows);
+        return w3 ? band_fits_t<double, MODEL_ORTHO, DAMP_W3D, false>(h, rows) : band_fits_t<double, MODEL_ORTHO, DAMP_SEP, false>(h, rows);
     }
 }
 
@@ -1432,6 +1473,33 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
     if (steps < 1) return ewf_fail(EWF_ERR_ARG, "nt too small to tune");
     if (h->nsrc > 0 && h->nstf < (size_t)steps + 1) return ewf_fail(EWF_ERR_STATE, "source time function too short");
     float best = 1e30f;
+    if (h->fused) {
+        // one-pass step: kernel (0: tile kernel, 4 / 8: band kernel rows per CTA) x z-chunk (each
+        // chunk recomputes two extra stress planes, so longer chunks than the other forms')
+        static const int bcand[] = {8, 16, 24, 32, 48, 64, 96, 128};
+        static const int rows_cand[] = {0, 4, 8};
+        int best_rows = h->band, best_kc = h->kchunk;
+        for (int rows : rows_cand) {
+            if (rows > 0 && !band_fits(h, rows)) continue;
+            for (int kc : bcand) {
+                if (kc > h->p.nz && kc != bcand[0]) continue;
+                h->band = rows;
+                h->kchunk = std::max(4, std::min(kc, h->p.nz));
+                float ms = 0.f;
+                if ((st = time_setting(h, steps, &ms))) return st;
+                if (ms >= 0.f && ms < best) {
+                    best = ms;
+                    best_rows = rows;
+                    best_kc = h->kchunk;
+                }
+            }
+        }
+        h->band = best_rows;
+        h->kchunk = best_kc;
+        h->graph_dirty = true;
+        if (kchunk) *kchunk = best_kc;
+        return ewf_reset(h);
+    }
     int best_k = h->kchunk, best_lag = h->wave_lag_pct, best_ty = h->ty;
     // wavefront step: slabs of 4..16 planes x lag (100000: every stress item before the first velocity item)
     static const int lag_pct[] = {50, 100, 200, 100000};
@@ -1529,6 +1597,26 @@ extern "C" int ewf_get_dependent_launch(const ewf_handle *h, int32_t *on)
 {
     if (!h || !on) return ewf_fail(EWF_ERR_ARG, "NULL argument");
     *on = h->pdl ? 1 : 0;
+    return EWF_OK;
+}
+
+extern "C" int ewf_set_band(ewf_handle *h, int32_t rows)
+{
+    if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
+    if (!h->fused) return ewf_fail(EWF_ERR_STATE, "the band height applies to the one-pass step");
+    if (rows != 0 && rows != 4 && rows != 8) return ewf_fail(EWF_ERR_ARG, "rows must be 0, 4 or 8 (got %d)", rows);
+    if (rows > 0 && !band_fits(h, rows))
+        return ewf_fail(EWF_ERR_UNSUPPORTED, "band kernel with %d rows: not built for this precision, more than %d CTAs of "
+                        "%d columns per band, or no cluster of that size fits the device", rows, BAND_MAX_CTAS, BX);
+    h->band = rows;
+    h->graph_dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_get_band(const ewf_handle *h, int32_t *rows)
+{
+    if (!h || !rows) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *rows = h->band;
     return EWF_OK;
 }
 

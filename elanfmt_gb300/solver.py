@@ -77,6 +77,8 @@ SIGNATURES = {
     "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_set_band": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_get_band": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_set_dependent_launch": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_l2_prefetch": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_l2_prefetch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
@@ -298,6 +300,16 @@ class Solver:
         ty = C.c_int32()
         _check(self._lib.ewf_get_tile(self._h, C.byref(ty)), "ewf_get_tile")
         return ty.value
+
+    def set_band(self, rows: int) -> None:
+        """One-pass step: rows per CTA of the band kernel (4 or 8; 0: the tile kernel that recomputes
+        the whole stress halo).  Results do not depend on it."""
+        _check(self._lib.ewf_set_band(self._h, int(rows)), "ewf_set_band")
+
+    def band(self) -> int:
+        v = C.c_int32()
+        _check(self._lib.ewf_get_band(self._h, C.byref(v)), "ewf_get_band")
+        return v.value
 
     def set_l2_prefetch(self, planes: int) -> None:
         """Two-kernel step: L2 prefetch distance of the velocity kernel (0 = off; results do not depend on it)."""

@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(built_lib):
 
 def test_abi_version_and_strerror(built_lib):
     lib = S.load_library()
-    assert lib.ewf_abi_version() == 5
+    assert lib.ewf_abi_version() == 6
     for code, name in F.STATUS.items():
         assert lib.ewf_strerror(code)
     assert lib.ewf_strerror(-99) == b"unknown status"
