@@ -46,6 +46,10 @@ KERNEL_BYTES = {
 }
 
 
+ONEPASS_NAMES = ["tile", "band4", "band8", "staged"]  # ewf_set_onepass values, in order
+ONEPASS_KERNELS = ["k_step", "k_band", "k_band", "k_staged"]
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -62,8 +66,8 @@ def parse():
     ap.add_argument("--kchunk", type=int, default=0, help="z-chunk / slab planes (0: autotuned)")
     ap.add_argument("--tile", type=int, default=0, help="CTA tile height in rows, with --kchunk (0: autotuned)")
     ap.add_argument("--l2pf", type=int, default=0, help="velocity kernel's L2 prefetch distance, with --kchunk --tile")
-    ap.add_argument("--band", type=int, default=-1,
-                    help="one-pass step: rows per band CTA (4, 8; 0: the tile kernel), with --kchunk (-1: autotuned)")
+    ap.add_argument("--onepass", default="", choices=["", "tile", "band4", "band8", "staged"],
+                    help="one-pass step: its kernel, with --kchunk (default: autotuned)")
     ap.add_argument("--wave-lag", type=int, default=0, help="wavefront lag in %% of the CTAs (0: autotuned)")
     ap.add_argument("--batch-iso", type=int, default=16, help="batch workload: isotropic models beside the 6 MTs")
     ap.add_argument("--no-reference", action="store_true", help="batch workload: skip the reference kernels' runs")
@@ -427,8 +431,8 @@ def main():
     if form == F.STEP_SPLIT and args.kchunk and args.tile:
         s.set_tile(args.tile)
         s.set_l2_prefetch(args.l2pf)
-    if form == F.STEP_FUSED and args.kchunk and args.band >= 0:
-        s.set_band(args.band)
+    if form == F.STEP_FUSED and args.kchunk and args.onepass:
+        s.set_onepass(ONEPASS_NAMES.index(args.onepass))
 
     for _ in range(args.warmup):
         s.reset()
@@ -459,7 +463,7 @@ def main():
                    **({"tile_y_autotuned": s.tile(), "l2_prefetch_autotuned": s.l2_prefetch()}
                       if form == F.STEP_SPLIT else {}),
                    **({"wave_lag_pct": s.wave_lag()} if form == F.STEP_WAVE else {}),
-                   **({"band_rows": s.band()} if form == F.STEP_FUSED else {})},
+                   **({"onepass_kernel": ONEPASS_NAMES[s.onepass()]} if form == F.STEP_FUSED else {})},
         "gpu_launches": launches,
     }
     step_frac = value * STEP_BYTES[args.workload] / peak
@@ -477,7 +481,7 @@ def main():
             names = {"stress": "k_stress", "velocity": "k_velocity"}
         else:  # one kernel does the whole step: its compulsory bytes are the one-pass step's
             kb = {"stress": STEP_BYTES[args.workload]}
-            names = {"stress": "k_wave" if form == F.STEP_WAVE else ("k_band" if s.band() > 0 else "k_step")}
+            names = {"stress": "k_wave" if form == F.STEP_WAVE else ONEPASS_KERNELS[s.onepass()]}
         kernels = {}
         for k in kb:
             achieved = kb[k] * m.cells / (kt[k] * 1e-3) / 1e9

@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
-    units = [("ewfd.cu", "ewfd.o"), ("ewfd_batch.cu", "ewfd_batch.o"), ("ewfd_band.cu", "ewfd_band.o"), ("ewf_mlp.cu", "ewf_mlp.o"),
+    units = [("ewfd.cu", "ewfd.o"), ("ewfd_batch.cu", "ewfd_batch.o"), ("ewfd_band.cu", "ewfd_band.o"), ("ewfd_staged.cu", "ewfd_staged.o"), ("ewf_mlp.cu", "ewf_mlp.o"),
              ("ewfd_post.cu", "ewfd_post.o"), ("ewfd_legacy.cpp", "ewfd_legacy.o")]
     cmds = []
     for src, obj in units:

@@ -10,6 +10,7 @@
 #include "ewfd_kernels.cuh"
 #include "ewfd_fused.cuh"
 #include "ewfd_band.h"
+#include "ewfd_staged.h"
 #include "ewfd_wave.cuh"
 
 #include <algorithm>
@@ -20,6 +21,7 @@
 #include <map>
 #include <mutex>
 #include <thread>
+#include <type_traits>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -183,7 +185,8 @@ struct ewf_handle {
     void *f_alloc[9] = {};
     void *g_alloc[9] = {};  // second state buffer of the fused step
     bool fused = false;
-    int band = 0;           // one-pass step: rows per band CTA of the cluster kernel (k_band); 0: k_step
+    int onepass = EWF_ONEPASS_TILE;  // one-pass step: its kernel (k_step, k_band with 4 / 8 rows, k_staged)
+    StagedPlan *splan = nullptr;     // tensor maps of the staged kernel (encoded on first use)
     bool dbuf = false;      // double-buffered state (one-pass step)
     int flip = 0;           // double-buffered: the current state is in g_alloc when 1
     bool wave = false;      // wavefront step (ewfd_wave.cuh)
@@ -474,6 +477,7 @@ extern "C" void ewf_destroy(ewf_handle *h)
     cudaFree(h->d_rcol);
     cudaFree(h->d_rent);
     cudaFree(h->d_stage);
+    delete h->splan;
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -523,6 +527,8 @@ static int validate_params(const ewf_params *p)
 }
 
 static bool band_fits(const ewf_handle *h, int rows);
+// rows per CTA of the band kernel for a one-pass kernel choice (0: not the band kernel)
+static int band_rows(int onepass) { return onepass == EWF_ONEPASS_BAND4 ? 4 : (onepass == EWF_ONEPASS_BAND8 ? 8 : 0); }
 
 extern "C" int ewf_create(const ewf_params *p, ewf_handle **out)
 {
@@ -1078,8 +1084,17 @@ static void fused_entry(const ewf_handle *h, cudaEvent_t *ev, int parity)
     fa.it_ptr = h->d_it;
     fa.order = h->p.src_order;
     if (ev) cudaEventRecord(ev[0], h->stream);
-    if (h->band > 0) {
-        band_launch<T, MODEL, DAMP, KAHAN>(fa, h->band, band_grid(h->p.nx, h->p.ny, h->p.nz, h->band, fa.a.kchunk), h->stream);
+    const int rows = band_rows(h->onepass);
+    bool staged = false;
+    if constexpr (std::is_same<T, float>::value && !KAHAN) {
+        if (h->onepass == EWF_ONEPASS_STAGED) {
+            staged_launch<MODEL, DAMP>(fa, *h->splan, parity, h->hx, h->stream);
+            staged = true;
+        }
+    }
+    if (staged) {
+    } else if (rows > 0) {
+        band_launch<T, MODEL, DAMP, KAHAN>(fa, rows, band_grid(h->p.nx, h->p.ny, h->p.nz, rows, fa.a.kchunk), h->stream);
     } else {
         const dim3 blk(FX, FY);
         const dim3 grd((h->p.nx + FX - 1) / FX, (h->p.ny + FY - 1) / FY, (h->p.nz + fa.a.kchunk - 1) / fa.a.kchunk);
@@ -1258,6 +1273,27 @@ static bool band_fits_t(const ewf_handle *h, int rows)
     return n >= 1;
 }
 
+// Can the staged kernel run on this handle (FP32 without compensation, models 0 and 1 with the
+// one-pass form's dampings, shared memory on this device, tensor maps of its allocations)?
+// Encodes the maps on first use.
+static bool staged_fits(ewf_handle *h)
+{
+    const ewf_params &p = h->p;
+    if (!h->fused || p.precision != EWF_PREC_F32 || p.damping == EWF_DAMP_PERCOMP || p.model == EWF_MODEL_ISO_HET) return false;
+    const bool iso = p.model == EWF_MODEL_ISO, w3 = p.damping == EWF_DAMP_W3D;
+    const bool ready = iso ? staged_ready<MODEL_ISO, DAMP_PML1D>()
+                           : (w3 ? staged_ready<MODEL_ORTHO, DAMP_W3D>() : staged_ready<MODEL_ORTHO, DAMP_SEP>());
+    if (!ready) return false;
+    if (!h->splan) {
+        h->splan = new (std::nothrow) StagedPlan();
+        if (!h->splan) return false;
+        static const int slots[9] = {0, 1, 2, 3, 4, 5, 6, 7, 8};
+        staged_encode(*h->splan, h->f_alloc, h->g_alloc, h->m_alloc, h->w3_alloc, iso ? 2 : 9, slots, !iso && w3, !iso,
+                      h->sx, p.ny, p.nz);
+    }
+    return h->splan->ok;
+}
+
 static bool band_fits(const ewf_handle *h, int rows)
 {
     const ewf_params &p = h->p;
@@ -1290,6 +1326,8 @@ static int step_prepare(ewf_handle *h)
 }
 static int step_check(ewf_handle *h)
 {
+    if (h->fused && h->onepass == EWF_ONEPASS_STAGED && staged_take_error())
+        return ewf_fail(EWF_ERR_CUDA, "staged one-pass step: a wait for a plane stage gave up; the state of this run is invalid");
     return wave_check(h);
 }
 
@@ -1477,24 +1515,25 @@ extern "C" int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk)
         // one-pass step: kernel (0: tile kernel, 4 / 8: band kernel rows per CTA) x z-chunk (each
         // chunk recomputes two extra stress planes, so longer chunks than the other forms')
         static const int bcand[] = {8, 16, 24, 32, 48, 64, 96, 128};
-        static const int rows_cand[] = {0, 4, 8};
-        int best_rows = h->band, best_kc = h->kchunk;
-        for (int rows : rows_cand) {
-            if (rows > 0 && !band_fits(h, rows)) continue;
+        static const int kern_cand[] = {EWF_ONEPASS_TILE, EWF_ONEPASS_BAND4, EWF_ONEPASS_BAND8, EWF_ONEPASS_STAGED};
+        int best_kern = h->onepass, best_kc = h->kchunk;
+        for (int kern : kern_cand) {
+            if (band_rows(kern) > 0 && !band_fits(h, band_rows(kern))) continue;
+            if (kern == EWF_ONEPASS_STAGED && !staged_fits(h)) continue;
             for (int kc : bcand) {
                 if (kc > h->p.nz && kc != bcand[0]) continue;
-                h->band = rows;
+                h->onepass = kern;
                 h->kchunk = std::max(4, std::min(kc, h->p.nz));
                 float ms = 0.f;
                 if ((st = time_setting(h, steps, &ms))) return st;
                 if (ms >= 0.f && ms < best) {
                     best = ms;
-                    best_rows = rows;
+                    best_kern = kern;
                     best_kc = h->kchunk;
                 }
             }
         }
-        h->band = best_rows;
+        h->onepass = best_kern;
         h->kchunk = best_kc;
         h->graph_dirty = true;
         if (kchunk) *kchunk = best_kc;
@@ -1600,23 +1639,30 @@ extern "C" int ewf_get_dependent_launch(const ewf_handle *h, int32_t *on)
     return EWF_OK;
 }
 
-extern "C" int ewf_set_band(ewf_handle *h, int32_t rows)
+extern "C" int ewf_set_onepass(ewf_handle *h, int32_t kernel)
 {
     if (!h) return ewf_fail(EWF_ERR_ARG, "NULL handle");
-    if (!h->fused) return ewf_fail(EWF_ERR_STATE, "the band height applies to the one-pass step");
-    if (rows != 0 && rows != 4 && rows != 8) return ewf_fail(EWF_ERR_ARG, "rows must be 0, 4 or 8 (got %d)", rows);
+    if (!h->fused) return ewf_fail(EWF_ERR_STATE, "the one-pass kernel applies to the one-pass step");
+    if (kernel < EWF_ONEPASS_TILE || kernel > EWF_ONEPASS_STAGED) return ewf_fail(EWF_ERR_ARG, "unknown one-pass kernel %d", kernel);
+    const int rows = band_rows(kernel);
     if (rows > 0 && !band_fits(h, rows))
         return ewf_fail(EWF_ERR_UNSUPPORTED, "band kernel with %d rows: not built for this precision, more than %d CTAs of "
                         "%d columns per band, or no cluster of that size fits the device", rows, BAND_MAX_CTAS, BX);
-    h->band = rows;
+    if (kernel == EWF_ONEPASS_STAGED) {
+        cudaSetDevice(h->device);
+        if (!staged_fits(h))
+            return ewf_fail(EWF_ERR_UNSUPPORTED, "staged kernel: built for FP32 without compensation and models 0 and 1; "
+                            "needs ~220 KB of shared memory per block and the driver's tensor-map encoder");
+    }
+    h->onepass = kernel;
     h->graph_dirty = true;
     return EWF_OK;
 }
 
-extern "C" int ewf_get_band(const ewf_handle *h, int32_t *rows)
+extern "C" int ewf_get_onepass(const ewf_handle *h, int32_t *kernel)
 {
-    if (!h || !rows) return ewf_fail(EWF_ERR_ARG, "NULL argument");
-    *rows = h->band;
+    if (!h || !kernel) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *kernel = h->onepass;
     return EWF_OK;
 }
 

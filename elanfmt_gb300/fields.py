@@ -12,6 +12,7 @@ import numpy as np
 MODEL_ISO, MODEL_ORTHO, MODEL_ISO_HET = 0, 1, 2
 PREC_F32, PREC_F32_KAHAN, PREC_F64 = 0, 1, 2
 STEP_SPLIT, STEP_FUSED, STEP_WAVE = 0, 1, 2   # ewf_params.fused: the step form
+ONEPASS_TILE, ONEPASS_BAND4, ONEPASS_BAND8, ONEPASS_STAGED = 0, 1, 2, 3  # ewf_set_onepass: the one-pass kernel
 DAMP_PML1D, DAMP_W3D, DAMP_SEPARABLE, DAMP_PERCOMP = 0, 1, 2, 3
 SRC_BEFORE_BC1, SRC_AFTER_BC1 = 0, 1
 FS_BC1, FS_NONE = 0, 1   # ewf_params.free_surface

@@ -77,8 +77,8 @@ SIGNATURES = {
     "ewf_set_wave": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_wave": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
-    "ewf_set_band": (C.c_int, [C.c_void_p, C.c_int32]),
-    "ewf_get_band": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ewf_set_onepass": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_get_onepass": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_set_dependent_launch": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_l2_prefetch": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_l2_prefetch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
@@ -301,14 +301,14 @@ class Solver:
         _check(self._lib.ewf_get_tile(self._h, C.byref(ty)), "ewf_get_tile")
         return ty.value
 
-    def set_band(self, rows: int) -> None:
-        """One-pass step: rows per CTA of the band kernel (4 or 8; 0: the tile kernel that recomputes
-        the whole stress halo).  Results do not depend on it."""
-        _check(self._lib.ewf_set_band(self._h, int(rows)), "ewf_set_band")
+    def set_onepass(self, kernel: int) -> None:
+        """One-pass step: its kernel, F.ONEPASS_TILE (default), F.ONEPASS_BAND4 / F.ONEPASS_BAND8 or
+        F.ONEPASS_STAGED.  Results do not depend on it."""
+        _check(self._lib.ewf_set_onepass(self._h, int(kernel)), "ewf_set_onepass")
 
-    def band(self) -> int:
+    def onepass(self) -> int:
         v = C.c_int32()
-        _check(self._lib.ewf_get_band(self._h, C.byref(v)), "ewf_get_band")
+        _check(self._lib.ewf_get_onepass(self._h, C.byref(v)), "ewf_get_onepass")
         return v.value
 
     def set_l2_prefetch(self, planes: int) -> None:

@@ -71,8 +71,8 @@ typedef enum ewf_damping {
 typedef enum ewf_step_form {
     EWF_STEP_SPLIT = 0, /* stress kernel, injection, velocity kernel (reference order OK4:485-498) */
     EWF_STEP_FUSED = 1, /* one-pass step kernel, double-buffered state (models 0 and 1): tiles
-                         * that recompute their stress halo, or bands of full-width rows, one
-                         * thread-block cluster each (ewf_set_band) */
+                         * that recompute their stress halo, bands of full-width rows (one
+                         * thread-block cluster each) or TMA-staged tiles (ewf_set_onepass) */
     EWF_STEP_WAVE = 2   /* one persistent launch of the stress and velocity updates over tile x slab
                          * items in dependency order, in place: the velocity update reads the new
                          * stresses back from L2 (every model, damping and precision) */
@@ -219,16 +219,26 @@ int ewf_autotune(ewf_handle *h, int32_t nsteps, int32_t *kchunk);
  * z-chunk; results do not depend on it.  ewf_set_tile: EWF_ERR_STATE for the other step forms. */
 int ewf_set_tile(ewf_handle *h, int32_t tile_y);
 int ewf_get_tile(const ewf_handle *h, int32_t *tile_y);
-/* One-pass step (fused = EWF_STEP_FUSED): rows per CTA of the band kernel.  4 or 8 (8: FP32
- * only): each band of full-width rows is one thread-block cluster of CTAs of 64 columns that hand
- * their stress edge columns to each other through distributed shared memory and recompute only
- * the band's y halo; it needs nx <= 16 * 64 and a cluster that fits the device.  0 (the
- * default): the tile kernel that recomputes the whole stress halo (any grid).  ewf_autotune
- * picks among 0, 4 and 8 with the z-chunk.  EWF_ERR_UNSUPPORTED where the band kernel cannot
- * run, EWF_ERR_STATE for the other step forms.  Results do not depend on it.
- * (Replaces nothing in the reference: its time loop is the two-launch step, OK4:485-505.) */
-int ewf_set_band(ewf_handle *h, int32_t rows);
-int ewf_get_band(const ewf_handle *h, int32_t *rows);
+/* One-pass step (fused = EWF_STEP_FUSED): the kernel that runs it.
+ *   EWF_ONEPASS_TILE (default): tiles of 32 x 8 columns that recompute their stress halo (any grid,
+ *     every precision);
+ *   EWF_ONEPASS_BAND4 / _BAND8: bands of 4 / 8 full-width rows, each one thread-block cluster of
+ *     CTAs of 64 columns that hand their stress edge columns to each other through distributed
+ *     shared memory (nx <= 16 * 64; BAND8 in FP32 only);
+ *   EWF_ONEPASS_STAGED: tiles of 64 x 8 columns whose planes (with their halo) are staged in
+ *     shared memory by TMA copies two planes ahead; the stress ring the velocity update reads is
+ *     recomputed from the staged plane (FP32 without compensation).
+ * ewf_autotune picks the kernel with the z-chunk.  EWF_ERR_UNSUPPORTED where a kernel cannot run,
+ * EWF_ERR_STATE for the other step forms.  Results do not depend on it.  (Replaces nothing in the
+ * reference: its time loop is the two-launch step, OK4:485-505.) */
+typedef enum ewf_onepass {
+    EWF_ONEPASS_TILE = 0,
+    EWF_ONEPASS_BAND4 = 1,
+    EWF_ONEPASS_BAND8 = 2,
+    EWF_ONEPASS_STAGED = 3
+} ewf_onepass;
+int ewf_set_onepass(ewf_handle *h, int32_t kernel);
+int ewf_get_onepass(const ewf_handle *h, int32_t *kernel);
 /* Two-kernel step: launch each kernel as a programmatic dependent of the previous one (1, the
  * default), so its CTAs are scheduled while the previous kernel finishes instead of after a launch
  * gap; every kernel still waits for the previous grid before it touches the state.  0: plain

@@ -18,11 +18,14 @@ pytestmark = pytest.mark.gpu
 ERR_ARG, ERR_STATE, ERR_UNSUPPORTED = -1, -5, -8  # ewf_status
 
 
+KERNEL = {0: F.ONEPASS_TILE, 4: F.ONEPASS_BAND4, 8: F.ONEPASS_BAND8}
+
+
 def run_band(m, nsteps, rows, prec=F.PREC_F32, kchunk=0, chunks=None, graph_steps=0):
     dt = np.float64 if prec == F.PREC_F64 else np.float32
     with Solver.from_model(m, precision=prec, fused=F.STEP_FUSED, kchunk=kchunk, graph_steps=graph_steps) as s:
-        s.set_band(rows)
-        assert s.band() == rows
+        s.set_onepass(KERNEL[rows])
+        assert s.onepass() == KERNEL[rows]
         for n in (chunks or [nsteps]):
             s.run(n)
         return [s.field(q, dt) for q in F.STATE], s.seismograms()
@@ -61,7 +64,7 @@ def test_band_nine_ctas(cuda_device):
     m = I.random_small(F.MODEL_ORTHO, 576, 13, 10, nt=12, seed=21, damping=F.DAMP_W3D)
     with Solver.from_model(m, fused=F.STEP_FUSED) as s:
         try:
-            s.set_band(4)
+            s.set_onepass(F.ONEPASS_BAND4)
         except EwfError:
             pytest.skip("no cluster of 9 CTAs fits this device")
     ref = O.run(m, 12)
@@ -97,36 +100,43 @@ def test_band_default_and_limits(cuda_device):
     form and the grid width."""
     m = I.random_small(F.MODEL_ORTHO, 96, 12, 8, nt=4, seed=2, damping=F.DAMP_W3D)
     with Solver.from_model(m, fused=F.STEP_FUSED) as s:
-        assert s.band() == 0  # the tile kernel by default
-        s.set_band(4)
-        assert s.band() == 4
+        assert s.onepass() == F.ONEPASS_TILE  # the tile kernel by default
+        s.set_onepass(F.ONEPASS_BAND4)
+        assert s.onepass() == F.ONEPASS_BAND4
         with pytest.raises(EwfError) as e:
-            s.set_band(3)
+            s.set_onepass(4)
         assert e.value.status == ERR_ARG
-        s.set_band(0)
-        assert s.band() == 0
+        s.set_onepass(F.ONEPASS_TILE)
+        assert s.onepass() == F.ONEPASS_TILE
     with Solver.from_model(m, fused=F.STEP_FUSED, precision=F.PREC_F64) as s:
         with pytest.raises(EwfError) as e:
-            s.set_band(8)  # FP64: 4 rows only
+            s.set_onepass(F.ONEPASS_BAND8)  # FP64: 4 rows only
+        assert e.value.status == ERR_UNSUPPORTED
+        with pytest.raises(EwfError) as e:
+            s.set_onepass(F.ONEPASS_STAGED)  # FP32 only
+        assert e.value.status == ERR_UNSUPPORTED
+    with Solver.from_model(m, fused=F.STEP_FUSED, precision=F.PREC_F32_KAHAN) as s:
+        with pytest.raises(EwfError) as e:
+            s.set_onepass(F.ONEPASS_STAGED)  # no compensation
         assert e.value.status == ERR_UNSUPPORTED
     with Solver.from_model(m) as s:  # two-kernel step
         with pytest.raises(EwfError) as e:
-            s.set_band(4)
+            s.set_onepass(F.ONEPASS_BAND4)
         assert e.value.status == ERR_STATE
     wide = I.random_small(F.MODEL_ORTHO, 1100, 4, 4, nt=2, seed=2, damping=F.DAMP_W3D)
-    with Solver.from_model(wide, fused=F.STEP_FUSED) as s:  # 18 CTAs per band: the tile kernel only
+    with Solver.from_model(wide, fused=F.STEP_FUSED) as s:  # 18 CTAs per band: not the band kernel
         with pytest.raises(EwfError) as e:
-            s.set_band(4)
+            s.set_onepass(F.ONEPASS_BAND4)
         assert e.value.status == ERR_UNSUPPORTED
+        s.set_onepass(F.ONEPASS_STAGED)  # tiles: any width
 
 
 def test_band_autotune_keeps_results(cuda_device):
-    """The autotuner chooses among the tile kernel and both band heights; the pick gives the
-    oracle's bits."""
+    """The autotuner chooses among the tile, band and staged kernels; the pick gives the oracle's
+    bits."""
     m = I.random_small(F.MODEL_ORTHO, 140, 24, 30, nt=24, seed=13, damping=F.DAMP_SEPARABLE)
     ref = O.run(m, 24)
     with Solver.from_model(m, fused=F.STEP_FUSED) as s:
         s.autotune(4)
-        assert s.band() in (0, 4, 8)
         s.run(24)
-        assert_bitwise(([s.field(q, np.float32) for q in F.STATE], s.seismograms()), ref, f"autotuned band {s.band()}")
+        assert_bitwise(([s.field(q, np.float32) for q in F.STATE], s.seismograms()), ref, f"autotuned kernel {s.onepass()}")
