@@ -20,18 +20,26 @@ from . import inputs as I
 from .solver import Solver
 
 
-def errors(a: np.ndarray, ref: np.ndarray) -> dict:
+def errors(a: np.ndarray, ref: np.ndarray, floor: float = 1e-3) -> dict:
+    """Per-trace errors of `a` against `ref`.  A trace whose reference norm is below `floor` times
+    the largest trace norm has seen no arrival yet (only the grid's numerical precursor, at the
+    rounding level): its relative error has no meaning, so it is counted apart and left out."""
     l2, peak = [], []
+    norms = np.linalg.norm(ref, axis=1)
+    cut = floor * norms.max() if len(norms) else 0.0
+    below = 0
     for r in range(len(ref)):
-        n = np.linalg.norm(ref[r])
+        n = norms[r]
         pk = np.max(np.abs(ref[r]))
-        if n == 0 or pk == 0:
+        if n == 0 or pk == 0 or n < cut:
+            below += 1
             continue
         l2.append(float(np.linalg.norm(a[r] - ref[r]) / n))
         peak.append(float(abs(np.max(np.abs(a[r])) - pk) / pk))
     l2 = np.array(l2)
     peak = np.array(peak)
-    return {"traces": int(len(l2)), "rel_l2_max": float(l2.max()), "rel_l2_median": float(np.median(l2)),
+    return {"traces": int(len(l2)), "traces_without_arrival": below, "norm_floor": floor,
+            "rel_l2_max": float(l2.max()), "rel_l2_median": float(np.median(l2)),
             "rel_l2_mean": float(l2.mean()), "peak_err_max": float(peak.max()),
             "peak_err_median": float(np.median(peak)), "rel_l2_per_trace": [float(v) for v in l2]}
 
