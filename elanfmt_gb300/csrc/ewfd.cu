@@ -1659,6 +1659,12 @@ extern "C" int ewf_set_onepass(ewf_handle *h, int32_t kernel)
     return EWF_OK;
 }
 
+extern "C" int ewf_staged_test_hold(int32_t plane, int32_t polls)
+{
+    if (staged_test_hold(plane, polls)) return ewf_fail(EWF_ERR_CUDA, "staged test hook: %s", cudaGetErrorString(cudaGetLastError()));
+    return EWF_OK;
+}
+
 extern "C" int ewf_get_onepass(const ewf_handle *h, int32_t *kernel)
 {
     if (!h || !kernel) return ewf_fail(EWF_ERR_ARG, "NULL argument");

@@ -92,6 +92,15 @@ cudaError_t staged_launch(const FusedArgs<float> &fa, const StagedPlan &plan, in
     return cudaPeekAtLastError();
 }
 
+int staged_test_hold(int plane, int polls)
+{
+    const int h = plane >= 0 ? plane : -1;
+    const int v = (plane >= 0 && polls > 0) ? polls : kStagedWaitPolls;
+    if (cudaMemcpyToSymbol(g_staged_wait_limit, &v, sizeof(int)) != cudaSuccess) return -1;
+    if (cudaMemcpyToSymbol(g_staged_hold, &h, sizeof(int)) != cudaSuccess) return -1;
+    return 0;
+}
+
 bool staged_take_error()
 {
     int v = 0;

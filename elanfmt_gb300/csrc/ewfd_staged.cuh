@@ -31,6 +31,8 @@ namespace ewf {
 
 __device__ int g_staged_err = 0;
 constexpr int kStagedWaitPolls = 1 << 22;
+__device__ int g_staged_wait_limit = kStagedWaitPolls;  // polls before a wait gives up
+__device__ int g_staged_hold = -1;  // test hook: plane whose copies the first CTA never issues (-1: none)
 
 __device__ __forceinline__ unsigned su32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void st_mbar_init(unsigned bar, unsigned count)
@@ -46,14 +48,16 @@ __device__ __forceinline__ bool st_mbar_try(unsigned bar, unsigned parity)
                  : "memory");
     return ok != 0;
 }
-// Bounded wait for a plane stage; gives up at once when another wait has already given up.
-__device__ __forceinline__ void st_mbar_wait(unsigned bar, unsigned parity)
+// Bounded wait for a plane stage (limit: g_staged_wait_limit, read once per launch); gives up at
+// once when another wait has already given up.
+__device__ __forceinline__ bool st_mbar_wait(unsigned bar, unsigned parity, int limit)
 {
-    for (int n = 0; n < kStagedWaitPolls; ++n) {
-        if (st_mbar_try(bar, parity)) return;
-        if ((n & 1023) == 1023 && *(volatile int *)&g_staged_err) return;
+    for (int n = 0; n < limit; ++n) {
+        if (st_mbar_try(bar, parity)) return true;
+        if ((n & 1023) == 1023 && *(volatile int *)&g_staged_err) return false;
     }
     atomicExch(&g_staged_err, 1);
+    return false;
 }
 __device__ __forceinline__ void st_mbar_expect(unsigned bar, unsigned bytes)
 {
@@ -190,8 +194,27 @@ __global__ void __launch_bounds__(SX *SY, 1) k_staged(const __grid_constant__ St
     const bool row_bc = (j < a.bc1_rows);
 
     // plane q into stage q % 3 (thread 0)
+    // the test hook and the wait limit, read once (they do not change during a launch)
+    const int wait_limit = *(volatile int *)&g_staged_wait_limit;
+    const int held_plane = (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0) ? *(volatile int *)&g_staged_hold : -1;
+    // thread 0's record of the fills it issued per stage (each completes one mbarrier phase): bit s
+    // of filled = at least one, of odd = an odd number; waits_ok = none of its waits gave up
+    unsigned filled = 0, odd = 0;
+    bool waits_ok = true;
+    // the last fill of stage s has landed (bounded wait on its phase)
+    auto drain_stage = [&](int s) {
+        const unsigned par = ((odd >> s) & 1u) ^ 1u;
+        for (int n = 0; n < wait_limit; ++n)
+            if (st_mbar_try(su32(&full[s]), par)) break;
+    };
     auto issue = [&](int q) {
+        if (q == held_plane) return;  // test hook: a fill nothing completes
         const int s = q % SNSTAGE;
+        // never two fills of one stage in flight on its mbarrier: once a wait has given up, the
+        // stage's previous fill may still be landing
+        if (!waits_ok && ((filled >> s) & 1u)) drain_stage(s);
+        filled |= 1u << s;
+        odd ^= 1u << s;
         float *st = stages + s * L::STAGE_FLOATS;
         const unsigned bar = su32(&full[s]);
         st_mbar_expect(bar, L::TX_BYTES);
@@ -286,8 +309,9 @@ __global__ void __launch_bounds__(SX *SY, 1) k_staged(const __grid_constant__ St
         if (tid == 0 && p + 2 <= plast) issue(p + 2);  // the stage of plane p-1: free since the last barrier
         const float *Sp = stages + (p % SNSTAGE) * L::STAGE_FLOATS;
         const float *Sn = stages + ((p + 1) % SNSTAGE) * L::STAGE_FLOATS;
-        st_mbar_wait(su32(&full[p % SNSTAGE]), (unsigned)((p - ps) / SNSTAGE) & 1u);
-        st_mbar_wait(su32(&full[(p + 1) % SNSTAGE]), (unsigned)((p + 1 - ps) / SNSTAGE) & 1u);
+        bool got = st_mbar_wait(su32(&full[p % SNSTAGE]), (unsigned)((p - ps) / SNSTAGE) & 1u, wait_limit);
+        got = st_mbar_wait(su32(&full[(p + 1) % SNSTAGE]), (unsigned)((p + 1 - ps) / SNSTAGE) & 1u, wait_limit) && got;
+        waits_ok = waits_ok && got;
 
         T sv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
         T xz1 = T(0), yz1 = T(0);
@@ -462,11 +486,11 @@ __global__ void __launch_bounds__(SX *SY, 1) k_staged(const __grid_constant__ St
         szz_m = sv[2];
     }
     // A wait that gave up may leave copies in flight: before the CTA's shared memory goes away,
-    // thread 0 waits for the last fill of every stage (a fixed bound: issued copies complete).
-    if (tid == 0 && *(volatile int *)&g_staged_err) {
-        for (int q = max(ps, plast - 2); q <= plast; ++q)
-            for (int n = 0; n < kStagedWaitPolls; ++n)
-                if (st_mbar_try(su32(&full[q % SNSTAGE]), (unsigned)((q - ps) / SNSTAGE) & 1u)) break;
+    // thread 0 waits (bounded) until every stage has completed one phase per fill it issued --
+    // issued copies always land, so this ends as soon as they have.
+    if (tid == 0 && (!waits_ok || *(volatile int *)&g_staged_err)) {
+        for (int s = 0; s < SNSTAGE; ++s)
+            if ((filled >> s) & 1u) drain_stage(s);
     }
 }
 

@@ -51,4 +51,8 @@ cudaError_t staged_launch(const FusedArgs<float> &fa, const StagedPlan &plan, in
 // the state written by that run is invalid).  Call after the stream has been synchronised.
 bool staged_take_error();
 
+// Test hook (ewf_staged_test_hold): the first CTA never issues the copies of plane `plane` and
+// every wait gives up after `polls` polls; plane < 0 restores normal operation.  0 or -1 (CUDA error).
+int staged_test_hold(int plane, int polls);
+
 }  // namespace ewf

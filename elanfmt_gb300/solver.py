@@ -79,6 +79,7 @@ SIGNATURES = {
     "ewf_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_onepass": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_onepass": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ewf_staged_test_hold": (C.c_int, [C.c_int32, C.c_int32]),
     "ewf_set_dependent_launch": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_set_l2_prefetch": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_get_l2_prefetch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),

@@ -239,6 +239,12 @@ typedef enum ewf_onepass {
 } ewf_onepass;
 int ewf_set_onepass(ewf_handle *h, int32_t kernel);
 int ewf_get_onepass(const ewf_handle *h, int32_t *kernel);
+/* Test hook of the staged kernel's failure path: with plane >= 0, the first CTA of every later
+ * staged launch never issues the copies of that plane (a stage fill nothing completes) and every
+ * wait for a plane stage gives up after `polls` polls; the launch still ends and ewf_run returns
+ * EWF_ERR_CUDA (the state of that run is invalid; the handle stays usable after ewf_reset).
+ * plane < 0 restores normal operation (default limit 2^22 polls). */
+int ewf_staged_test_hold(int32_t plane, int32_t polls);
 /* Two-kernel step: launch each kernel as a programmatic dependent of the previous one (1, the
  * default), so its CTAs are scheduled while the previous kernel finishes instead of after a launch
  * gap; every kernel still waits for the previous grid before it touches the state.  0: plain

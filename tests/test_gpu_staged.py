@@ -82,3 +82,26 @@ def test_staged_free_surface_sources(cuda_device):
                     m.set_moment_tensor(np.array([1.0, -0.5, 0.25, 0.7, -0.9, 1.3]), 63, 7, zs, stencil)
                     ref = O.run(m, 30)
                     assert_bitwise(run_staged(m, 30), ref, f"model {model} order {order} stencil {stencil} zs {zs}")
+
+
+def test_staged_wait_gives_up_and_handle_recovers(cuda_device):
+    """A stage fill that nothing completes (test hook): the bounded waits give up, the launch still
+    ends, ewf_run reports EWF_ERR_CUDA; after the hook is cleared and the state reset, the next run
+    is bit-exact."""
+    from elanfmt_gb300.solver import EwfError, load_library
+
+    lib = load_library()
+    m = I.random_small(F.MODEL_ORTHO, 70, 20, 24, nt=12, seed=41, damping=F.DAMP_SEPARABLE)
+    ref = O.run(m, 12)
+    with Solver.from_model(m, fused=F.STEP_FUSED, kchunk=8, graph_steps=-1) as s:
+        s.set_onepass(F.ONEPASS_STAGED)
+        assert lib.ewf_staged_test_hold(5, 4096) == 0
+        try:
+            with pytest.raises(EwfError) as e:
+                s.run(3)
+            assert e.value.status == -2  # EWF_ERR_CUDA
+        finally:
+            assert lib.ewf_staged_test_hold(-1, 0) == 0
+        s.reset()
+        s.run(12)
+        assert_bitwise(([s.field(q, np.float32) for q in F.STATE], s.seismograms()), ref, "after the failed run")
