@@ -337,12 +337,13 @@ def extra_batch(nt: int = 300) -> dict:
         b.run(nt)
         b.reset()
         batch_s = b.run(nt) * 1e-3
-        setting = (b.tile(),)
+        setting = (b.tile(), b.l2_prefetch())
     solo_s = solo_seconds(probs, nt)
     return {"workload": f"6 elementary MTs on orthorhombic 256^3 + 16 isotropic models 96^3-224^3, {nt} steps "
                         f"(the full workload runs 3000)", "runs": runs, "batched_runs_per_s": round(runs / batch_s, 3),
             "solo_runs_per_s": round(runs / solo_s, 3), "speedup_vs_solo": round(solo_s / batch_s, 3),
-            "batch_tile_y": setting[0], "solo": "each run alone with its own autotuned z-chunk and tile height"}
+            "batch_tile_y": setting[0], "batch_l2_prefetch": setting[1],
+            "solo": "each run alone with its own autotuned z-chunk and tile height"}
 
 
 def extra_precision(nt: int = 2000) -> dict:
@@ -602,6 +603,7 @@ def main_batch(args):
         else:
             k = b.autotune(10)
         tile = b.tile()
+        l2pf = b.l2_prefetch()
         clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
         clk.start()
         ms_batch = [b.run(nt)]
@@ -623,7 +625,8 @@ def main_batch(args):
            "solo": "each run alone with its own autotuned z-chunk and tile height",
            "batched_gcell_updates_per_s": round(cell_updates / batch_s / 1e9, 2),
            "solo_gcell_updates_per_s": round(cell_updates / solo_s / 1e9, 2),
-           "kchunk_autotuned": k, "tile_y_autotuned": tile, "dtype": "f32", "data": "synthetic (seeded)",
+           "kchunk_autotuned": k, "tile_y_autotuned": tile, "l2_prefetch_autotuned": l2pf, "dtype": "f32",
+           "data": "synthetic (seeded)",
            "config": {"workload": f"6 elementary MTs on orthorhombic {n_ortho}^3 + {args.batch_iso} isotropic models "
                                   f"96^3-224^3, {nt} steps",
                       "runs": runs, "cell_updates": cell_updates}}

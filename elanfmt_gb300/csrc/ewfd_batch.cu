@@ -98,6 +98,7 @@ struct ewf_batch {
     size_t stage_bytes = 0;
     bool dirty = true;   // device tables need a rebuild
     int ty = TY;         // CTA tile height in rows of 32 columns (autotuned; 4, 8 or 16)
+    int l2pf = 0;        // multi-RHS velocity kernel: L2 prefetch distance of its state inputs (autotuned; 0 = off)
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 64;
     float last_ms = 0.f;
@@ -436,6 +437,7 @@ static int build_tables(ewf_batch *b)
         d.bc1 = p.free_surface == EWF_FS_BC1 ? 1 : 0;
         d.smu_on = p.surface_mu > 0.0 ? 1 : 0;
         d.smu = (float)p.surface_mu;
+        d.l2pf = q.R > 1 ? b->l2pf : 0;
         bp.tiles_x = (p.nx + TX - 1) / TX;
         bp.tiles_y = (p.ny + b->ty - 1) / b->ty;
         bp.chunks = (p.nz + q.kchunk - 1) / q.kchunk;
@@ -724,9 +726,31 @@ extern "C" int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk_
         CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
         if (ms < best) { best = ms; best_k = kc; best_ty = ty; }
     }
-    for (auto &e : ev) cudaEventDestroy(e);
     for (auto &q : b->probs) q.kchunk = std::max(4, std::min(best_k, q.p.nz));
     b->ty = best_ty;
+    // then the multi-RHS velocity kernel's L2 prefetch distance at that setting
+    int best_pf = 0;
+    if (!b->mr.empty()) {
+        static const int pf_cand[] = {0, 2, 3, 4};
+        float best_pf_ms = 1e30f;
+        for (int pf : pf_cand) {
+            b->l2pf = pf;
+            b->dirty = true;
+            int st = batch_ready(b);
+            if (!st) st = ewf_batch_reset(b);
+            if (st) { for (auto &e : ev) cudaEventDestroy(e); return st; }
+            batch_step(b, nullptr);  // warm
+            CK(cudaEventRecord(b->ev0, b->stream));
+            for (int s = 1; s < std::min(nsteps + 1, b->nt); ++s) batch_step(b, nullptr);
+            CK(cudaEventRecord(b->ev1, b->stream));
+            CK(cudaStreamSynchronize(b->stream));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            if (ms < best_pf_ms) { best_pf_ms = ms; best_pf = pf; }
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    b->l2pf = best_pf;
     b->dirty = true;
     int st = batch_ready(b);
     if (st) return st;
@@ -740,6 +764,22 @@ extern "C" int ewf_batch_set_tile(ewf_batch *b, int32_t tile_y)
     if (tile_y != 4 && tile_y != 8 && tile_y != 16) return ewf_fail(EWF_ERR_ARG, "tile_y must be 4, 8 or 16 (got %d)", tile_y);
     b->ty = tile_y;
     b->dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_batch_set_l2_prefetch(ewf_batch *b, int32_t planes)
+{
+    if (!b) return ewf_fail(EWF_ERR_ARG, "NULL batch");
+    if (planes < 0 || planes > 8) return ewf_fail(EWF_ERR_ARG, "planes must be in [0, 8] (got %d)", planes);
+    b->l2pf = planes;
+    b->dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_batch_get_l2_prefetch(const ewf_batch *b, int32_t *planes)
+{
+    if (!b || !planes) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *planes = b->l2pf;
     return EWF_OK;
 }
 

@@ -117,8 +117,9 @@ __global__ void __launch_bounds__(TX * BATCH_MAX_TY, 2) k_velocity_mr(const Step
     const int r = blockIdx.x % R;
     const int tx = blockIdx.x / R;
     const int k0 = blockIdx.z * a.kchunk;
-    velocity_column<T, MODEL, DAMP, false, 1, true>(a, tx * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y, k0,
-                                                 min(k0 + a.kchunk, a.nz), (long long)r * rhs_stride);
+    // REC: the L2 prefetch of the state inputs a.l2pf planes ahead (no receivers: col_first is null)
+    velocity_column<T, MODEL, DAMP, false, 1, true, 0, true>(a, tx * TX + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y,
+                                                          k0, min(k0 + a.kchunk, a.nz), (long long)r * rhs_stride, RecFuse{});
 }
 
 // Point injection for every (problem, RHS): one thread per (problem, RHS), entries in order,

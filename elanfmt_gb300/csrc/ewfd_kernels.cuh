@@ -618,12 +618,15 @@ __device__ __forceinline__ void vel_store(const StepArgs<T> &a, long long c, int
 // compensation where the scheme reads them) that holds the row's cells.  This returns lane l's
 // field (null: none); the row's line of plane k is at field + (c - lane) + k * plane pitch, c
 // being the lane's element (the x pitch and the row start are 32-aligned).  (The stress kernel,
-// already at the copy bandwidth, has no registers to spare for it.)
-template <typename T, int MODEL, int DAMP, bool KAHAN>
+// already at the copy bandwidth, has no registers to spare for it.)  STATE_ONLY: the state fields
+// alone (a right-hand side in a box of its own, soff elements after the materials' index: c is
+// the state's index, and the shared material lines come from L2 for all right-hand sides).
+template <typename T, int MODEL, int DAMP, bool KAHAN, bool STATE_ONLY = false>
 __device__ __forceinline__ const T *vel_prefetch_field(const StepArgs<T> &a, int lane)
 {
     if (lane < 6) return a.f[3 + lane];
     if (lane < 9) return a.f[lane - 6];
+    if (STATE_ONLY) return nullptr;
     if (MODEL != MODEL_ISO && lane < 12) return a.m[lane];
     if (MODEL != MODEL_ISO && DAMP == DAMP_W3D && lane == 12) return a.w3;
     if (MODEL == MODEL_ISO && DAMP == DAMP_PERCOMP && lane >= 9 && lane < 12) return a.w6[lane - 9];
@@ -656,7 +659,7 @@ __device__ __forceinline__ void velocity_column(const StepArgs<T> &a, int X, int
     // the L2 prefetch's field for this lane (REC: the two-kernel step's velocity kernel)
     const T *pf_row = nullptr;
     if (REC && a.l2pf > 0) {
-        pf_row = vel_prefetch_field<T, MODEL, DAMP, KAHAN>(a, (int)threadIdx.x);
+        pf_row = vel_prefetch_field<T, MODEL, DAMP, KAHAN, SOFF>(a, (int)threadIdx.x);
         if (pf_row) pf_row += c - (long long)threadIdx.x + (long long)a.l2pf * sys;
     }
     // receivers on this column (REC: the two-kernel step's velocity kernel)

@@ -103,6 +103,8 @@ SIGNATURES = {
     "ewf_batch_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "ewf_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_batch_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    "ewf_batch_set_l2_prefetch": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_batch_get_l2_prefetch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_mlp_gemm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "ewf_mlp_status": (C.c_int, []),
@@ -486,6 +488,15 @@ class Batch:
         ty = C.c_int32()
         _check(self._lib.ewf_batch_get_tile(self._h, C.byref(ty)), "ewf_batch_get_tile")
         return ty.value
+
+    def set_l2_prefetch(self, planes: int) -> None:
+        """Multi-RHS problems: L2 prefetch distance of their velocity kernel (0 = off; results do not depend on it)."""
+        _check(self._lib.ewf_batch_set_l2_prefetch(self._h, int(planes)), "ewf_batch_set_l2_prefetch")
+
+    def l2_prefetch(self) -> int:
+        v = C.c_int32()
+        _check(self._lib.ewf_batch_get_l2_prefetch(self._h, C.byref(v)), "ewf_batch_get_l2_prefetch")
+        return v.value
 
     def seismograms(self, prob: int, rhs: int) -> np.ndarray:
         m = self.models[prob]

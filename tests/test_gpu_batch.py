@@ -83,6 +83,28 @@ def test_batch_tile_heights(cuda_device):
                 b.set_tile(bad)
 
 
+def test_batch_l2_prefetch(cuda_device):
+    """The multi-RHS velocity kernel's L2 prefetch is a hint: every distance gives the same bits."""
+    probs = problems(nt=24)
+    ref = None
+    for pf in (0, 2, 5):
+        with Batch(probs) as b:
+            b.set_l2_prefetch(pf)
+            assert b.l2_prefetch() == pf
+            b.run(24)
+            got = [[b.seismograms(p, r) for r in range(len(rl))] + [b.field(p, 0, F.F_VX)]
+                   for p, (_, rl) in enumerate(probs)]
+        if ref is None:
+            ref = got
+        else:
+            for a, c in zip(got, ref):
+                for x, y in zip(a, c):
+                    np.testing.assert_array_equal(x, y, err_msg=f"prefetch {pf}")
+    with Batch(probs) as b:
+        with pytest.raises(Exception):
+            b.set_l2_prefetch(9)
+
+
 def test_batch_graph_autotune_and_reset(cuda_device):
     probs = problems(nt=140)
     with Batch(probs) as b:
