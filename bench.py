@@ -337,12 +337,13 @@ def extra_batch(nt: int = 300) -> dict:
         b.run(nt)
         b.reset()
         batch_s = b.run(nt) * 1e-3
-        setting = (b.tile(), b.l2_prefetch())
+        setting = (b.tile(), b.l2_prefetch(), b.launch())
     solo_s = solo_seconds(probs, nt)
     return {"workload": f"6 elementary MTs on orthorhombic 256^3 + 16 isotropic models 96^3-224^3, {nt} steps "
                         f"(the full workload runs 3000)", "runs": runs, "batched_runs_per_s": round(runs / batch_s, 3),
             "solo_runs_per_s": round(runs / solo_s, 3), "speedup_vs_solo": round(solo_s / batch_s, 3),
             "batch_tile_y": setting[0], "batch_l2_prefetch": setting[1],
+            "batch_launch": "own launches on parallel branches" if setting[2] else "persistent family launch",
             "solo": "each run alone with its own autotuned z-chunk and tile height"}
 
 
@@ -604,6 +605,7 @@ def main_batch(args):
             k = b.autotune(10)
         tile = b.tile()
         l2pf = b.l2_prefetch()
+        own = b.launch()
         clk = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
         clk.start()
         ms_batch = [b.run(nt)]
@@ -625,7 +627,8 @@ def main_batch(args):
            "solo": "each run alone with its own autotuned z-chunk and tile height",
            "batched_gcell_updates_per_s": round(cell_updates / batch_s / 1e9, 2),
            "solo_gcell_updates_per_s": round(cell_updates / solo_s / 1e9, 2),
-           "kchunk_autotuned": k, "tile_y_autotuned": tile, "l2_prefetch_autotuned": l2pf, "dtype": "f32",
+           "kchunk_autotuned": k, "tile_y_autotuned": tile, "l2_prefetch_autotuned": l2pf,
+           "launch_autotuned": "own launches on parallel branches" if own else "persistent family launch", "dtype": "f32",
            "data": "synthetic (seeded)",
            "config": {"workload": f"6 elementary MTs on orthorhombic {n_ortho}^3 + {args.batch_iso} isotropic models "
                                   f"96^3-224^3, {nt} steps",

@@ -99,6 +99,12 @@ struct ewf_batch {
     bool dirty = true;   // device tables need a rebuild
     int ty = TY;         // CTA tile height in rows of 32 columns (autotuned; 4, 8 or 16)
     int l2pf = 0;        // multi-RHS velocity kernel: L2 prefetch distance of its state inputs (autotuned; 0 = off)
+    bool own = false;    // every problem gets launches of its own, on BRANCHES parallel streams (autotuned);
+                         // false: the single-RHS problems of a family share one persistent launch
+    static constexpr int BRANCHES = 4;
+    cudaStream_t branch[BRANCHES] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[BRANCHES] = {};
+    std::vector<int> branch_of;  // per entry of mr: its branch (balanced by cell-updates)
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 64;
     float last_ms = 0.f;
@@ -142,6 +148,11 @@ extern "C" void ewf_batch_destroy(ewf_batch *b)
     cudaFree(b->d_stage);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+    for (auto &e : b->join_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &x : b->branch)
+        if (x) cudaStreamDestroy(x);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -188,6 +199,11 @@ extern "C" int ewf_batch_create(int32_t n, const ewf_params *p, const int32_t *n
     CKB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CKB(cudaEventCreate(&b->ev0));
     CKB(cudaEventCreate(&b->ev1));
+    CKB(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+    for (int k = 0; k < ewf_batch::BRANCHES; ++k) {
+        CKB(cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking));
+        CKB(cudaEventCreateWithFlags(&b->join_ev[k], cudaEventDisableTiming));
+    }
     for (int i = 0; i < n; ++i) {
         Prob &q = b->probs[i];
         q.p = p[i];
@@ -437,7 +453,7 @@ static int build_tables(ewf_batch *b)
         d.bc1 = p.free_surface == EWF_FS_BC1 ? 1 : 0;
         d.smu_on = p.surface_mu > 0.0 ? 1 : 0;
         d.smu = (float)p.surface_mu;
-        d.l2pf = q.R > 1 ? b->l2pf : 0;
+        d.l2pf = (q.R > 1 || b->own) ? b->l2pf : 0;
         bp.tiles_x = (p.nx + TX - 1) / TX;
         bp.tiles_y = (p.ny + b->ty - 1) / b->ty;
         bp.chunks = (p.nz + q.kchunk - 1) / q.kchunk;
@@ -448,7 +464,7 @@ static int build_tables(ewf_batch *b)
     b->mr.clear();
     std::map<std::pair<int, int>, int> fam_of;
     for (int i = 0; i < n; ++i) {
-        if (b->probs[i].R > 1) {
+        if (b->probs[i].R > 1 || b->own) {
             b->mr.push_back(i);
             continue;
         }
@@ -459,6 +475,23 @@ static int build_tables(ewf_batch *b)
             b->fams.back().ty = b->ty;
         }
         b->fams[fam_of[key]].probs.push_back(i);
+    }
+    // branches of the own launches: largest problems first, each to the least loaded branch
+    b->branch_of.assign(b->mr.size(), 0);
+    {
+        std::vector<int> idx(b->mr.size());
+        for (size_t e = 0; e < idx.size(); ++e) idx[e] = (int)e;
+        auto work = [&](int e) {
+            const Prob &q = b->probs[b->mr[e]];
+            return (double)q.p.nx * q.p.ny * q.p.nz * q.R;
+        };
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return work(x) > work(y); });
+        double load[ewf_batch::BRANCHES] = {};
+        for (int e : idx) {
+            const int k = (int)(std::min_element(load, load + ewf_batch::BRANCHES) - load);
+            b->branch_of[e] = k;
+            load[k] += work(e);
+        }
     }
     for (auto &f : b->fams) {
         std::vector<BatchProb<float>> v;
@@ -574,14 +607,28 @@ static void batch_step(ewf_batch *b, cudaEvent_t *ev)
 {
     cudaStream_t s = b->stream;
     if (ev) cudaEventRecord(ev[0], s);
-    for (int i : b->mr) launch_mr(b, i, true, s);
+    // the own launches of one phase: on one stream, or forked over the branch streams and joined
+    auto own_phase = [&](bool stress) {
+        if (!b->own || b->mr.size() < 2) {
+            for (int i : b->mr) launch_mr(b, i, stress, s);
+            return;
+        }
+        cudaEventRecord(b->fork_ev, s);
+        for (auto &x : b->branch) cudaStreamWaitEvent(x, b->fork_ev, 0);
+        for (size_t e = 0; e < b->mr.size(); ++e) launch_mr(b, b->mr[e], stress, b->branch[b->branch_of[e]]);
+        for (int k = 0; k < ewf_batch::BRANCHES; ++k) {
+            cudaEventRecord(b->join_ev[k], b->branch[k]);
+            cudaStreamWaitEvent(s, b->join_ev[k], 0);
+        }
+    };
+    own_phase(true);
     for (auto &f : b->fams) launch_family(f, true, s);
     if (ev) cudaEventRecord(ev[1], s);
     if (b->d_src)
         k_binject<float><<<(b->ngroups + 127) / 128, 128, 0, s>>>(b->d_all, b->d_src, b->d_src_start, b->ngroups, b->d_stf,
                                                                   b->d_stf_off, b->d_order, b->nt, b->d_it);
     if (ev) cudaEventRecord(ev[2], s);
-    for (int i : b->mr) launch_mr(b, i, false, s);
+    own_phase(false);
     for (auto &f : b->fams) launch_family(f, false, s);
     if (ev) cudaEventRecord(ev[3], s);
     if (b->nrec_total)
@@ -706,12 +753,15 @@ extern "C" int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk_
     static const int ty_cand[] = {4, 8, 16};
     float best = 1e30f;
     int best_k = 16, best_ty = b->ty;
+    bool best_own = b->own;
     cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (int own = 0; own < 2; ++own)
     for (int ty : ty_cand)
     for (int kc : cand) {
         for (auto &q : b->probs) q.kchunk = std::max(4, std::min(kc, q.p.nz));
         b->ty = ty;
+        b->own = own != 0;
         b->dirty = true;
         int st = batch_ready(b);
         if (st) { for (auto &e : ev) cudaEventDestroy(e); return st; }
@@ -724,10 +774,13 @@ extern "C" int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk_
         CK(cudaStreamSynchronize(b->stream));
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-        if (ms < best) { best = ms; best_k = kc; best_ty = ty; }
+        if (ms < best) { best = ms; best_k = kc; best_ty = ty; best_own = own != 0; }
     }
     for (auto &q : b->probs) q.kchunk = std::max(4, std::min(best_k, q.p.nz));
     b->ty = best_ty;
+    b->own = best_own;
+    b->dirty = true;
+    if (int st = batch_ready(b)) { for (auto &e : ev) cudaEventDestroy(e); return st; }
     // then the multi-RHS velocity kernel's L2 prefetch distance at that setting
     int best_pf = 0;
     if (!b->mr.empty()) {
@@ -764,6 +817,22 @@ extern "C" int ewf_batch_set_tile(ewf_batch *b, int32_t tile_y)
     if (tile_y != 4 && tile_y != 8 && tile_y != 16) return ewf_fail(EWF_ERR_ARG, "tile_y must be 4, 8 or 16 (got %d)", tile_y);
     b->ty = tile_y;
     b->dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_batch_set_launch(ewf_batch *b, int32_t own)
+{
+    if (!b) return ewf_fail(EWF_ERR_ARG, "NULL batch");
+    if (own != 0 && own != 1) return ewf_fail(EWF_ERR_ARG, "own must be 0 or 1 (got %d)", own);
+    b->own = own != 0;
+    b->dirty = true;
+    return EWF_OK;
+}
+
+extern "C" int ewf_batch_get_launch(const ewf_batch *b, int32_t *own)
+{
+    if (!b || !own) return ewf_fail(EWF_ERR_ARG, "NULL argument");
+    *own = b->own ? 1 : 0;
     return EWF_OK;
 }
 

@@ -104,6 +104,8 @@ SIGNATURES = {
     "ewf_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int32]),
     "ewf_batch_get_tile": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_batch_set_l2_prefetch": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_batch_set_launch": (C.c_int, [C.c_void_p, C.c_int32]),
+    "ewf_batch_get_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_batch_get_l2_prefetch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "ewf_mlp_gemm": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
                                C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
@@ -488,6 +490,16 @@ class Batch:
         ty = C.c_int32()
         _check(self._lib.ewf_batch_get_tile(self._h, C.byref(ty)), "ewf_batch_get_tile")
         return ty.value
+
+    def set_launch(self, own: int) -> None:
+        """Single-RHS problems: 0 = one persistent launch per model family, 1 = launches of their own
+        on parallel branches (results do not depend on it)."""
+        _check(self._lib.ewf_batch_set_launch(self._h, int(own)), "ewf_batch_set_launch")
+
+    def launch(self) -> int:
+        v = C.c_int32()
+        _check(self._lib.ewf_batch_get_launch(self._h, C.byref(v)), "ewf_batch_get_launch")
+        return v.value
 
     def set_l2_prefetch(self, planes: int) -> None:
         """Multi-RHS problems: L2 prefetch distance of their velocity kernel (0 = off; results do not depend on it)."""

@@ -351,8 +351,8 @@ int ewf_batch_last_run_ms(const ewf_batch *b, double *ms);
 /* traces of (prob, rhs): out[r*nt + it] for the problem's n_rec receivers */
 int ewf_batch_get_seismograms(ewf_batch *b, int32_t prob, int32_t rhs, double *out, size_t n);
 int ewf_batch_get_field(ewf_batch *b, int32_t prob, int32_t rhs, int32_t field, void *host, size_t n, int32_t dtype_bytes);
-/* the autotuner over the whole batch: z-chunk and CTA tile height, then the multi-RHS velocity
- * kernel's L2 prefetch distance (leaves the batch reset) */
+/* the autotuner over the whole batch: launch form, z-chunk and CTA tile height, then the
+ * multi-RHS velocity kernel's L2 prefetch distance (leaves the batch reset) */
 int ewf_batch_autotune(ewf_batch *b, int32_t nsteps, int32_t *kchunk);
 /* CTA tile height of every launch of the batch, in rows of 32 columns: 4, 8 (default) or 16;
  * results do not depend on it */
@@ -362,6 +362,12 @@ int ewf_batch_get_tile(const ewf_batch *b, int32_t *tile_y);
  * ahead (0..8; 0 = off, the default; ewf_batch_autotune picks it).  A hint: results do not
  * depend on it. */
 int ewf_batch_set_l2_prefetch(ewf_batch *b, int32_t planes);
+/* Launch form of the single-RHS problems: 0 (default) -- those of one model family share one
+ * persistent launch per phase; 1 -- every problem gets launches of its own, spread over four
+ * parallel branches (streams of the captured graph) balanced by cell-updates.  Problems with
+ * several RHS always have their own launches.  Results do not depend on it. */
+int ewf_batch_set_launch(ewf_batch *b, int32_t own);
+int ewf_batch_get_launch(const ewf_batch *b, int32_t *own);
 int ewf_batch_get_l2_prefetch(const ewf_batch *b, int32_t *planes);
 
 /* ---------------------------------------------------------------------------------------------

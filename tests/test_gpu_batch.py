@@ -83,6 +83,28 @@ def test_batch_tile_heights(cuda_device):
                 b.set_tile(bad)
 
 
+def test_batch_launch_forms(cuda_device):
+    """Single-RHS problems in one persistent family launch or in launches of their own on parallel
+    graph branches: the same bits, graph replays included."""
+    probs = problems(nt=70)
+    ref = None
+    for own in (0, 1):
+        with Batch(probs) as b:
+            b.set_launch(own)
+            assert b.launch() == own
+            b.run(70)  # one graph of 64 steps + 6 direct steps
+            got = [[b.seismograms(p, r) for r in range(len(rl))] + [b.field(p, 0, F.F_SYY)]
+                   for p, (_, rl) in enumerate(probs)]
+        if ref is None:
+            ref = got
+            m, rl = probs[-1]
+            np.testing.assert_array_equal(got[-1][0], solo(m, rl[0][0], rl[0][1], 70)[1])
+        else:
+            for a, c in zip(got, ref):
+                for x, y in zip(a, c):
+                    np.testing.assert_array_equal(x, y, err_msg=f"launch form {own}")
+
+
 def test_batch_l2_prefetch(cuda_device):
     """The multi-RHS velocity kernel's L2 prefetch is a hint: every distance gives the same bits."""
     probs = problems(nt=24)
