@@ -114,3 +114,15 @@ def test_ewfd_executable_reports_errors(built_lib, tmp_path):
     assert "pa1.dat" in r.stderr
     r = subprocess.run([exe, "--bogus"], capture_output=True, text=True)
     assert r.returncode == 1
+
+
+def test_null_handles_are_rejected(built_lib):
+    """The launch-setting entry points answer a NULL handle with EWF_ERR_ARG (no device needed)."""
+    lib = S.load_library()
+    v = C.c_int32()
+    for name in ("ewf_set_onepass", "ewf_set_tile", "ewf_set_l2_prefetch", "ewf_set_dependent_launch", "ewf_set_wave",
+                 "ewf_batch_set_launch", "ewf_batch_set_l2_prefetch", "ewf_batch_set_tile"):
+        assert getattr(lib, name)(None, 0) == -1, name
+    for name in ("ewf_get_onepass", "ewf_get_tile", "ewf_get_l2_prefetch", "ewf_get_dependent_launch", "ewf_get_wave",
+                 "ewf_batch_get_launch", "ewf_batch_get_l2_prefetch", "ewf_batch_get_tile"):
+        assert getattr(lib, name)(None, C.byref(v)) == -1, name
