@@ -59,3 +59,23 @@ def test_full_run_seismograms_vs_reference_stock(cuda_device, make, step):
     assert np.abs(rt).max() > 0
     assert err["zero_mismatch"] == 0
     assert err["max_rel_l2"] <= TOL, err
+
+
+@pytest.mark.parametrize("make", [iso128, ortho320], ids=["iso128-1000steps", "ortho320x320x256-4000steps"])
+def test_step_forms_bit_identical_on_the_benchmark_workloads(cuda_device, make):
+    """Every step form and one-pass kernel reproduces the two-kernel step bit for bit on the full
+    benchmark workloads (so each meets the bar above), at the launch shapes of the autotuner's
+    range: the band kernel's clusters span the whole x extent (2 and 5 CTAs) and the staged
+    kernel's tiles are ragged on neither grid."""
+    m = make()
+    with Solver.from_model(m, fused=F.STEP_SPLIT) as s:
+        s.run(m.nt)
+        ref_traces = s.seismograms()
+        ref_vz = s.field(F.F_VZ)
+    assert np.abs(ref_traces).max() > 0
+    for kernel, kchunk in ((F.ONEPASS_STAGED, 32), (F.ONEPASS_BAND4, 32), (F.ONEPASS_TILE, 16)):
+        with Solver.from_model(m, fused=F.STEP_FUSED, kchunk=kchunk) as s:
+            s.set_onepass(kernel)
+            s.run(m.nt)
+            np.testing.assert_array_equal(s.seismograms(), ref_traces, err_msg=f"one-pass kernel {kernel}")
+            np.testing.assert_array_equal(s.field(F.F_VZ), ref_vz, err_msg=f"one-pass kernel {kernel}")
