@@ -10,7 +10,7 @@
  *   ewfd --nbx 12 --nby 12 --nbz 7 [--overx 0 ...] [--model iso|ortho|isohet|dcq] [--nt N] [--vdamp C]
  *        [--precision f32|kahan|f64] [--src i,j,k] [--stencil ok4|aniso] [--mts FILE]
  *        [--free-surface bc1|none] [--surface-mu MU]
- *        [--receivers FILE] [--snap-every N] [--workdir DIR] [--quiet] [--no-checks]
+ *        [--receivers FILE] [--snap-every N] [--autotune STEPS] [--workdir DIR] [--quiet] [--no-checks]
  *
  * --free-surface none drops BC1 (the diff_BC schemes comment its launch out); --surface-mu MU
  * gives the isotropic scheme's shear modulus MU on plane k = 1 (the diff_BC2_OK3 scheme: 1e-5).
@@ -69,7 +69,7 @@ int main(int argc, char **argv)
     ewf_params p;
     ewf_params_default(&p);
     int nbx = 0, nby = 0, nbz = 0, overx = 0, overy = 0, overz = 0;
-    int src[3] = {-1, -1, -1}, stencil = -1, snap_every = 0, quiet = 0, percomp = 0;
+    int src[3] = {-1, -1, -1}, stencil = -1, snap_every = 0, quiet = 0, percomp = 0, tune = 0;
     const char *mts_file = NULL, *rec_file = NULL;
     p.workdir = ".";
     p.nout = 200;
@@ -80,7 +80,7 @@ int main(int argc, char **argv)
         ARG_INT("--nbx", nbx) ARG_INT("--nby", nby) ARG_INT("--nbz", nbz)
         ARG_INT("--overx", overx) ARG_INT("--overy", overy) ARG_INT("--overz", overz)
         ARG_INT("--nx", p.nx) ARG_INT("--ny", p.ny) ARG_INT("--nz", p.nz) ARG_INT("--nt", p.nt)
-        ARG_INT("--snap-every", snap_every) ARG_INT("--kchunk", p.kchunk)
+        ARG_INT("--snap-every", snap_every) ARG_INT("--kchunk", p.kchunk) ARG_INT("--autotune", tune)
 #undef ARG_INT
         if (!strcmp(k, "--model") && v) {
             if (!strcmp(v, "ortho")) p.model = EWF_MODEL_ORTHO;
@@ -159,6 +159,11 @@ int main(int argc, char **argv)
         st = ewf_set_receivers(h, n, r);
         free(r);
         if (st) { ewf_destroy(h); return fail(st, "receivers"); }
+    }
+    if (tune > 0) {  /* the library's autotuner: launch shapes timed over `tune` steps, state reset after */
+        int32_t kc = 0;
+        if ((st = ewf_autotune(h, tune, &kc))) { ewf_destroy(h); return fail(st, "autotune"); }
+        if (!quiet) printf("autotuned over %d steps: z-chunk %d\n", tune, kc);
     }
     double total_ms = 0.0;
     int isave = 1;

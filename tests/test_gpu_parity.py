@@ -473,6 +473,15 @@ def test_legacy_file_contract_through_ewfd(cuda_device, tmp_path):
         np.testing.assert_array_equal(out[name], ref.traces[q].astype(np.float32))
     np.testing.assert_array_equal(out["Rec_all"], ref.traces.astype(np.float32))
     np.testing.assert_array_equal(out["Src"], m.stf[: m.nt].astype(np.float32))
+    # autotuned launch shapes (state reset after tuning): the same files, byte for byte
+    names = [f for f in os.listdir(tmp_path) if f.endswith(".res")]
+    before = {f: (tmp_path / f).read_bytes() for f in names}
+    r = subprocess.run([exe, "--nx", "40", "--ny", "44", "--nz", "24", "--workdir", str(tmp_path), "--src",
+                        f"{xs},{ys},{zs}", "--receivers", str(tmp_path / "rec.txt"), "--autotune", "6", "--quiet"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for f in names:
+        assert (tmp_path / f).read_bytes() == before[f], f
     # the same through the Python mirror of the executable
     s = Solver.legacy(str(tmp_path), 40, 44, 24)
     try:
