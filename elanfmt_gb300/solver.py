@@ -411,10 +411,14 @@ class Solver:
 
 
 def run_legacy(workdir: str, nx: int, ny: int, nz: int, model: int = F.MODEL_ISO, nt: int = 0,
-               precision: int = F.PREC_F32) -> float:
+               precision: int = F.PREC_F32, autotune: int = 0) -> float:
     """The reference executable end to end: read inputs from workdir, run all nt steps, write
-    0_infos.inf and 0_0_*.res.  Returns the device time in ms."""
+    0_infos.inf and 0_0_*.res.  Returns the device time in ms.  autotune > 0: the library's
+    autotuner first times launch shapes over that many steps (outputs unchanged), as
+    ``ewfd --autotune``."""
     with Solver.legacy(workdir, nx, ny, nz, model=model, nt=nt, precision=precision) as s:
+        if autotune > 0:
+            s.autotune(autotune)
         ms = s.run(s.params.nt)
         s.write_legacy_outputs()
     return ms
