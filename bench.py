@@ -601,6 +601,7 @@ def main_batch(args):
         if args.kchunk and args.tile:  # a fixed setting (profiling runs)
             k = args.kchunk
             b.set_tile(args.tile)
+            b.set_l2_prefetch(args.l2pf)
         else:
             k = b.autotune(10)
         tile = b.tile()
